@@ -1,0 +1,165 @@
+"""Regenerate the golden fixtures in this directory from the reference itself.
+
+Runs the CTSim 5.2.0 binaries compiled from the unmodified sources by
+``make -C oracle ref`` (oracle/_ref/ctsimtext with FP32 images as shipped,
+oracle/_ref/fp64/ctsimtext with IMAGEFILE_64_BITS, oracle/_ref/ref_harness
+for the filtered rows the CLIs do not write out) and stores their outputs as
+small compressed .npz files.  Needs the reference sources, so it runs only in
+the development container; the fixtures it writes are committed and travel.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from ctsim_gb300.fileio import read_if, read_pj  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref", "ctsimtext")
+REF64 = os.path.join(ROOT, "oracle", "_ref", "fp64", "ctsimtext")
+HARN = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+FILTERS = ["abs_bandlimit", "abs_hamming", "abs_hanning", "abs_cosine", "shepp", "abs_sinc",
+           "bandlimit", "sinc", "hamming", "hanning", "cosine", "triangle"]
+
+
+def run(*args):
+    subprocess.run([str(a) for a in args], check=True, stdout=subprocess.DEVNULL)
+
+
+def pj_arrays(prefix, pj):
+    return {prefix + "data": pj.data, prefix + "angles": pj.angles,
+            prefix + "hdr": np.array([pj.geometry, pj.nDet, pj.nView, pj.rotStart, pj.rotInc,
+                                      pj.detStart, pj.detInc, pj.viewDiameter, pj.focalLength,
+                                      pj.sourceDetectorLength, pj.fanBeamAngle], np.float64)}
+
+
+# (name, phantom, geometry, ndet, nview, nray, extra phm2pj args)
+SCANS = [
+    ("c1", "shepp-logan", "parallel", 367, 320, 2, []),
+    ("herman_par", "herman", "parallel", 101, 60, 2, []),
+    ("shepp_eqa", "shepp-logan", "equiangular", 133, 96, 1, []),
+    ("shepp_eqa_even", "shepp-logan", "equiangular", 134, 90, 3, []),
+    ("herman_eql", "herman", "equilinear", 128, 80, 2, []),
+    ("herman_eqa", "herman", "equiangular", 99, 72, 1, []),
+    ("shepp_par_even", "shepp-logan", "parallel", 64, 50, 1, ["--offsetview", "3"]),
+    ("pulse_par", "unit-pulse", "parallel", 65, 8, 1, []),
+    ("shepp_eql_ratio", "shepp-logan", "equilinear", 97, 64, 1,
+     ["--focal-length", "3", "--center-detector-length", "1.5", "--view-ratio", "1.2",
+      "--scan-ratio", "0.9"]),
+]
+
+
+def make_scans(tmp):
+    out = {}
+    for name, phm, geo, nd, nv, nr, extra in SCANS:
+        f = os.path.join(tmp, name + ".pj")
+        run(REF, "phm2pj", f, nd, nv, "--phantom", phm, "--geometry", geo, "--nray", nr, *extra)
+        out.update(pj_arrays(name + "/", read_pj(f)))
+    np.savez_compressed(os.path.join(HERE, "scans.npz"), **out)
+    return out
+
+
+# (scan, nx, ny, backproj, interp, filter, method, zeropad, generation, filter-param)
+RECONS = [("c1", 256, 256, "table", "linear", "abs_bandlimit", "convolution", 1, "direct", -1)]
+for bp in ("trig", "table", "diff", "idiff"):
+    for ip in ("nearest", "linear", "cubic"):
+        RECONS.append(("herman_par", 40, 40, bp, ip, "abs_bandlimit", "convolution", 1, "direct", -1))
+        RECONS.append(("shepp_par_even", 33, 31, bp, ip, "abs_hamming", "convolution", 1, "direct", 0.54))
+for ip in ("nearest", "linear", "cubic"):
+    for sc in ("shepp_eqa", "shepp_eqa_even", "herman_eql", "shepp_eql_ratio"):
+        RECONS.append((sc, 36, 36, "table", ip, "abs_hamming", "convolution", 1, "direct", 0.54))
+RECONS += [
+    ("shepp_eqa", 32, 32, "table", "cubic", "abs_hamming", "fourier", 2, "direct", 0.54),
+    ("shepp_eqa", 32, 32, "table", "cubic", "shepp", "fourier", 1, "direct", -1),
+    ("herman_eql", 32, 32, "table", "linear", "abs_cosine", "fouier-table", 1, "direct", -1),
+    ("herman_par", 32, 32, "idiff", "linear", "abs_bandlimit", "fourier", 0, "inverse-fourier", -1),
+    ("herman_par", 32, 32, "idiff", "linear", "abs_hanning", "convolution", 1, "inverse-fourier", -1),
+]
+
+
+def make_recons(tmp, scans):
+    out = {}
+    for k, (sc, nx, ny, bp, ip, flt, meth, zp, gen, prm) in enumerate(RECONS):
+        pjf = os.path.join(tmp, sc + ".pj")
+        args = ["pjrec", pjf, os.path.join(tmp, "r.if"), nx, ny, "--backproj", bp, "--interp", ip,
+                "--filter", flt, "--filter-method", meth, "--zeropad", zp,
+                "--filter-generation", gen]
+        if prm >= 0:
+            args += ["--filter-param", prm]
+        run(REF64, *args)
+        out["%d/image64" % k] = read_if(os.path.join(tmp, "r.if")).data
+        run(REF, *args)
+        out["%d/image32" % k] = read_if(os.path.join(tmp, "r.if")).data
+        out["%d/cfg" % k] = np.array([sc, nx, ny, bp, ip, flt, meth, zp, gen, prm], dtype=object)
+    np.savez_compressed(os.path.join(HERE, "recons.npz"), **out)
+
+
+def make_filters(tmp):
+    rng = np.random.default_rng(2024)
+    nd, nv = 29, 2
+    x = rng.random((nv, nd)).astype(np.float32)
+    fin = os.path.join(tmp, "fin.f32")
+    fout = os.path.join(tmp, "fout.f64")
+    x.tofile(fin)
+    out = {"input": x}
+    cases = []
+    for gid, fl, sdl in ((0, 0.0, 0.0), (1, 2.6, 5.2), (2, 2.6, 5.2)):
+        for f in FILTERS:
+            for m in ("convolution", "fourier", "fouier-table"):
+                for gen in ("direct", "inverse-fourier"):
+                    for zp in ((1,) if m == "convolution" else (0, 1, 2)):
+                        run(HARN, "filter", gid, nd, nv, repr(0.0123), repr(fl), repr(sdl), f, "0.54",
+                            m, zp, gen, 1, fin, fout)
+                        out["%d" % len(cases)] = np.fromfile(fout).reshape(nv, nd)
+                        cases.append((gid, fl, sdl, f, m, gen, zp))
+    out["cases"] = np.array(cases, dtype=object)
+    np.savez_compressed(os.path.join(HERE, "filters.npz"), **out)
+
+
+def make_helical(tmp):
+    out = {}
+    for k, (nd, nv, rot, iv) in enumerate([(101, 360, 3, -1), (64, 300, 2.5, 130)]):
+        f = os.path.join(tmp, "h.pj")
+        run(REF, "phm2pj", f, nd, nv, "--phantom", "herman", "--geometry", "equiangular",
+            "--nray", 1, "--rotangle", rot)
+        run(REF, "pjHinterp", f, os.path.join(tmp, "hi.pj"), "--interpview", iv)
+        out.update(pj_arrays("%d/in_" % k, read_pj(f)))
+        out.update(pj_arrays("%d/out_" % k, read_pj(os.path.join(tmp, "hi.pj"))))
+        out["%d/interpview" % k] = np.array(iv)
+    np.savez_compressed(os.path.join(HERE, "helical.npz"), **out)
+
+
+def make_raster(tmp):
+    out = {}
+    for k, (phm, n, ns) in enumerate([("herman", 48, 2), ("shepp-logan", 40, 3)]):
+        f = os.path.join(tmp, "p.if")
+        run(REF64, "phm2if", f, n, n, "--phantom", phm, "--nsample", ns)
+        out["%d/image" % k] = read_if(f).data
+        out["%d/cfg" % k] = np.array([phm, n, ns], dtype=object)
+    np.savez_compressed(os.path.join(HERE, "raster.npz"), **out)
+
+
+def main():
+    for b in (REF, REF64, HARN):
+        if not os.path.exists(b):
+            sys.exit("reference not built: run `make -C oracle ref`")
+    with tempfile.TemporaryDirectory() as tmp:
+        scans = make_scans(tmp)
+        make_recons(tmp, scans)
+        make_filters(tmp)
+        make_helical(tmp)
+        make_raster(tmp)
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print("%-14s %8d bytes" % (f, os.path.getsize(os.path.join(HERE, f))))
+
+
+if __name__ == "__main__":
+    main()

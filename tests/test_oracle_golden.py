@@ -1,0 +1,117 @@
+"""The FP64 oracle against the reference's own outputs (golden fixtures made by
+tests/golden/make_golden.py from CTSim compiled from source)."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+SCANS = ["c1", "herman_par", "shepp_eqa", "shepp_eqa_even", "herman_eql", "herman_eqa",
+         "shepp_par_even", "pulse_par", "shepp_eql_ratio"]
+SCAN_ARGS = {  # phantom, geometry, nray, extra Scanner kwargs (tests/golden/make_golden.py)
+    "c1": ("shepp-logan", "parallel", 2, {}),
+    "herman_par": ("herman", "parallel", 2, {}),
+    "shepp_eqa": ("shepp-logan", "equiangular", 1, {}),
+    "shepp_eqa_even": ("shepp-logan", "equiangular", 3, {}),
+    "herman_eql": ("herman", "equilinear", 2, {}),
+    "herman_eqa": ("herman", "equiangular", 1, {}),
+    "shepp_par_even": ("shepp-logan", "parallel", 1, {"offset_view": 3}),
+    "pulse_par": ("unit-pulse", "parallel", 1, {}),
+    "shepp_eql_ratio": ("shepp-logan", "equilinear", 1,
+                        {"fl_ratio": 3.0, "cd_ratio": 1.5, "view_ratio": 1.2, "scan_ratio": 0.9}),
+}
+
+
+def geom_from_hdr(po, hdr):
+    g, nd, nv, _rs, ri, _ds, di, vd, fl, sdl, fan = hdr
+    return po.Geom(int(g), int(nd), int(nv), ri, di, fl, sdl, vd, fan)
+
+
+@pytest.mark.parametrize("name", SCANS)
+def test_oracle_raysums_match_reference(oracle, golden, name):
+    d = golden("scans")
+    phm, geo, nray, kw = SCAN_ARGS[name]
+    hdr = d[name + "/hdr"]
+    sc = oracle.Scanner(oracle.Phantom(phm), geo, int(hdr[1]), int(hdr[2]), nsample=nray, **kw)
+    assert sc.detInc == hdr[6] and sc.viewDiameter == hdr[7] and sc.fanBeamAngle == hdr[10]
+    sino, ang = sc.collect()
+    np.testing.assert_array_equal(ang, d[name + "/angles"])
+    ref = d[name + "/data"]
+    # the reference stores FP32; the oracle's FP64 sums round to the same floats
+    mism = np.count_nonzero(sino.astype(np.float32) != ref)
+    assert mism <= max(1, ref.size // 100000), mism
+    assert rel_l2(sino, ref) < 1e-7
+
+
+def test_oracle_reconstructions_match_reference(oracle, golden):
+    scans = golden("scans")
+    rec = golden("recons")
+    n = len([k for k in rec.files if k.endswith("/cfg")])
+    for k in range(n):
+        sc, nx, ny, bp, ip, flt, meth, zp, gen, prm = rec["%d/cfg" % k]
+        g = geom_from_hdr(oracle, scans[sc + "/hdr"])
+        img = oracle.reconstruct(g, scans[sc + "/data"], scans[sc + "/angles"], int(nx), int(ny),
+                                 filter_name=flt, param=float(prm), method=meth, zeropad=int(zp),
+                                 generation=gen, backproj=bp, interp=ip)
+        ref = rec["%d/image64" % k]
+        scale = np.abs(ref).max()
+        np.testing.assert_allclose(img, ref, rtol=0, atol=1e-12 * scale,
+                                   err_msg="case %d %s" % (k, rec["%d/cfg" % k]))
+        # and the reference's shipped FP32-image build differs from FP64 only by rounding
+        assert rel_l2(rec["%d/image32" % k], ref) < 2e-6
+
+
+def test_oracle_filters_match_reference(oracle, golden):
+    d = golden("filters")
+    x = d["input"]
+    names = {0: "parallel", 1: "equiangular", 2: "equilinear"}
+    for k, (gid, fl, sdl, f, m, gen, zp) in enumerate(d["cases"]):
+        ps = oracle.ProcessSignal(f, m, x.shape[1], 0.0123, param=0.54, generation=gen,
+                                  zeropad=int(zp), geometry=names[int(gid)], focal_length=fl,
+                                  sdl=sdl)
+        out = ps.filter(x)
+        ref = d["%d" % k]
+        scale = max(np.abs(ref).max(), 1e-300)
+        np.testing.assert_allclose(out, ref, rtol=0, atol=1e-12 * scale,
+                                   err_msg="case %s" % (d["cases"][k],))
+
+
+def test_oracle_fft_method_equals_fourier(oracle):
+    rng = np.random.default_rng(5)
+    x = rng.random((3, 45)).astype(np.float32)
+    for geo in ("parallel", "equiangular", "equilinear"):
+        a = oracle.ProcessSignal("abs_hamming", "fourier", 45, 0.01, param=0.54, zeropad=2,
+                                 geometry=geo, focal_length=2.0, sdl=4.0).filter(x)
+        b = oracle.ProcessSignal("abs_hamming", "fft", 45, 0.01, param=0.54, zeropad=2,
+                                 geometry=geo, focal_length=2.0, sdl=4.0).filter(x)
+        np.testing.assert_allclose(b, a, rtol=0, atol=1e-11 * np.abs(a).max())
+
+
+def test_oracle_helical_matches_reference(oracle, golden):
+    d = golden("helical")
+    for k in range(2):
+        g = geom_from_hdr(oracle, d["%d/in_hdr" % k])
+        h, ang = oracle.helical180li(g, d["%d/in_data" % k], int(d["%d/interpview" % k]))
+        np.testing.assert_array_equal(ang, d["%d/out_angles" % k])
+        g.nView = h.shape[0]
+        f = oracle.halfscan_feather(g, h)
+        np.testing.assert_array_equal(f, d["%d/out_data" % k])
+
+
+def test_oracle_raster_matches_reference(oracle, golden):
+    d = golden("raster")
+    for k in range(2):
+        phm, n, ns = d["%d/cfg" % k]
+        img, _ = oracle.phantom_to_image(oracle.Phantom(phm), int(n), int(n), 1.0, int(ns))
+        np.testing.assert_allclose(img, d["%d/image" % k], rtol=0, atol=1e-12)
+
+
+def test_oracle_projector_is_adjoint_of_backprojector(oracle, golden):
+    scans = golden("scans")
+    g = geom_from_hdr(oracle, scans["herman_par/hdr"])
+    ang = scans["herman_par/angles"]
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((24, 20))
+    y = rng.standard_normal((len(ang), g.nDet))
+    ax = oracle.project_image(g, x, ang)
+    bty = oracle.backproject(g, y, ang, 24, 20, "table", "linear", post_process=False)
+    assert abs(np.vdot(ax, y) - np.vdot(x, bty)) < 1e-12 * abs(np.vdot(ax, y))
