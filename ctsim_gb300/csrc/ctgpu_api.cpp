@@ -1,0 +1,902 @@
+// ctgpu_api.cpp -- host core and C ABI of libctgpu.so (declared in include/ctgpu.h).
+//
+// The host side computes everything that is per-object or per-view and cheap,
+// in FP64 and in the reference's own order of operations (element transforms
+// and outline boxes, scanner geometry, the incrementally rotated view end
+// points, filter design, fixed-point backprojection steps), and launches the
+// sm_103a kernels for everything that is per ray, per detector sample or per
+// pixel.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <strings.h>
+#include <vector>
+
+#include "../../include/ctgpu.h"
+#include "ctgpu_internal.h"
+#include "filter_design.h"
+
+using namespace ctgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+int ok() {
+  g_err.clear();
+  return CTGPU_OK;
+}
+
+#define CUDA_TRY(expr)                                                              \
+  do {                                                                              \
+    cudaError_t e_ = (expr);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(CTGPU_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+cudaError_t ensure_device(T*& p, size_t& cap, size_t count) {
+  if (count <= cap && p) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), sizeof(T) * (count ? count : 1));
+  if (e == cudaSuccess) cap = count;
+  return e;
+}
+
+// ---- 2-D row-vector affine maps (libctsupport/xform.cpp:87-148) -----------
+struct M3 { double m[3][3]; };
+M3 ident() { M3 r{}; r.m[0][0] = r.m[1][1] = r.m[2][2] = 1; return r; }
+M3 xlat(double x, double y) { M3 r = ident(); r.m[2][0] = x; r.m[2][1] = y; return r; }
+M3 rotm(double t) {
+  M3 r = ident();
+  double c = std::cos(t), s = std::sin(t);
+  r.m[0][0] = c; r.m[0][1] = s; r.m[1][0] = -s; r.m[1][1] = c;
+  return r;
+}
+M3 mul(const M3& a, const M3& b) {
+  M3 r;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      r.m[i][j] = 0;
+      for (int k = 0; k < 3; k++) r.m[i][j] += a.m[i][k] * b.m[k][j];
+    }
+  return r;
+}
+void apply(const M3& m, double& x, double& y) {
+  double xt = x * m.m[0][0] + y * m.m[1][0] + m.m[2][0];
+  double yt = x * m.m[0][1] + y * m.m[1][1] + m.m[2][1];
+  x = xt;
+  y = yt;
+}
+
+int elem_type(const char* n) {   // libctsim/phantom.cpp:590-607
+  if (!strcasecmp(n, "rectangle")) return kRect;
+  if (!strcasecmp(n, "triangle")) return kTriangle;
+  if (!strcasecmp(n, "ellipse")) return kEllipse;
+  if (!strcasecmp(n, "sector")) return kSector;
+  if (!strcasecmp(n, "segment")) return kSegment;
+  return 0;
+}
+
+int circle_points(double theta) {   // phantom.cpp:821-827
+  theta = theta <= 0 ? 0 : (theta >= kTwoPi ? kTwoPi : theta);
+  return (int)(360 * theta / kTwoPi + 1.5);
+}
+
+void arc(std::vector<double>& x, std::vector<double>& y, int at, int pts, double xc, double yc,
+         double r, double start, double stop) {   // phantom.cpp:771-793
+  double th = (stop - start) / (pts - 1), c = std::cos(th), s = std::sin(th);
+  x[at] = r * std::cos(start) + xc;
+  y[at] = r * std::sin(start) + yc;
+  double xp = x[at] - xc, yp = y[at] - yc;
+  for (int i = 1; i < pts; i++) {
+    double xn = c * xp - s * yp, yn = s * xp + c * yp;
+    x[at + i] = xn + xc;
+    y[at + i] = yn + yc;
+    xp = xn;
+    yp = yn;
+  }
+}
+
+// PhantomElement: radians, and the bounding box of the outline polygon the
+// reference draws (phantom.cpp:554-566, :669-756); rays missing that box are
+// rejected before clipping.
+PElem make_elem(int type, double cx, double cy, double u, double v, double rotDeg, double atten) {
+  PElem e{};
+  e.type = type;
+  e.cx = cx; e.cy = cy; e.u = u; e.v = v; e.atten = atten;
+  e.rot = rotDeg * (kPi / 180.);
+  e.cosr = std::cos(e.rot);
+  e.sinr = std::sin(e.rot);
+  std::vector<double> x, y;
+  switch (type) {
+    case kRect:
+      x = {-u, u, u, -u, -u}; y = {-v, -v, v, v, -v};
+      break;
+    case kTriangle:
+      x = {-u, u, 0.0, -u}; y = {0.0, 0.0, v, 0.0};
+      break;
+    case kEllipse: {
+      int n = circle_points(kTwoPi);
+      x.resize(n); y.resize(n);
+      arc(x, y, 0, n, 0, 0, 1.0, 0.0, kTwoPi);
+      for (int i = 0; i < n; i++) { x[i] *= u; y[i] *= v; }
+      break;
+    }
+    case kSector: {
+      double r = std::sqrt(u * u + v * v), th = std::atan(u / v);
+      double start = 3.0 * kHalfPi - th, stop = 3.0 * kHalfPi + th;
+      int c = circle_points(stop - start);
+      x.resize(c + 3); y.resize(c + 3);
+      x[0] = 0.0; y[0] = v; x[1] = -u; y[1] = 0.0;
+      arc(x, y, 2, c, 0.0, v, r, start, stop);
+      x[c + 2] = 0.0; y[c + 2] = v;
+      break;
+    }
+    case kSegment: {
+      double r = std::sqrt(u * u + v * v), th = std::atan(u / v);
+      double start = 3.0 * kHalfPi - th, stop = 3.0 * kHalfPi + th;
+      int c = circle_points(stop - start);
+      x.resize(c + 1); y.resize(c + 1);
+      arc(x, y, 0, c, 0.0, v, r, start, stop);
+      x[c] = -u; y[c] = 0.0;
+      break;
+    }
+  }
+  double c = std::cos(e.rot), s = std::sin(e.rot);
+  for (size_t i = 0; i < x.size(); i++) {
+    double xr = x[i] * c - y[i] * s, yr = x[i] * s + y[i] * c;
+    x[i] = xr + cx;
+    y[i] = yr + cy;
+  }
+  e.bx0 = e.bx1 = x[0];
+  e.by0 = e.by1 = y[0];
+  for (size_t i = 1; i < x.size(); i++) {
+    e.bx0 = std::fmin(e.bx0, x[i]); e.bx1 = std::fmax(e.bx1, x[i]);
+    e.by0 = std::fmin(e.by0, y[i]); e.by1 = std::fmax(e.by1, y[i]);
+  }
+  return e;
+}
+
+int geometry_from_name(const char* n) {   // scanner.cpp:35-41, :254-265
+  if (!strcasecmp(n, "parallel")) return kParallel;
+  if (!strcasecmp(n, "equiangular")) return kEquiangular;
+  if (!strcasecmp(n, "equilinear")) return kEquilinear;
+  return -1;
+}
+int interp_from_name(const char* n) {   // backprojectors.cpp:73-96
+  if (!strcasecmp(n, "nearest")) return kNearest;
+  if (!strcasecmp(n, "linear")) return kLinear;
+  if (!strcasecmp(n, "cubic")) return kCubic;
+  return -1;
+}
+int backproj_from_name(const char* n) {   // backprojectors.cpp:34-46
+  if (!strcasecmp(n, "trig")) return kTrig;
+  if (!strcasecmp(n, "table")) return kTable;
+  if (!strcasecmp(n, "diff")) return kDiff;
+  if (!strcasecmp(n, "idiff")) return kIDiff;
+  return -1;
+}
+
+long long nearest_ll(double x) { return x > 0 ? (long long)(x + 0.5) : (long long)(x - 0.5); }
+
+int pitch_for(int nDet) { return (nDet + 3) & ~3; }
+
+}  // namespace
+
+// ===========================================================================
+struct ctgpu_phantom {
+  std::vector<PElem> elems;   // reference list order: last added first
+  double xmin = 1E30, xmax = -1E30, ymin = 1E30, ymax = -1E30;
+  bool unitPulse = false;
+  PElem* d_elems = nullptr;
+  size_t d_cap = 0;
+  bool dirty = true;
+
+  cudaError_t upload(cudaStream_t s) {
+    if (!dirty && d_elems) return cudaSuccess;
+    cudaError_t e = ensure_device(d_elems, d_cap, elems.size());
+    if (e != cudaSuccess) return e;
+    if (!elems.empty())
+      e = cudaMemcpyAsync(d_elems, elems.data(), sizeof(PElem) * elems.size(),
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    dirty = false;
+    return e;
+  }
+  ~ctgpu_phantom() { if (d_elems) cudaFree(d_elems); }
+};
+
+struct ctgpu_scanner {
+  int geometry, nDet, nView, offsetView, nSample;
+  double rotLen, rotInc, detInc, detLen, detStart;
+  double viewDiameter, scanDiameter, focalLength, centerDetectorLength, sourceDetectorLength;
+  double fanBeamAngle, xCenter, yCenter, angularDetLen = 0, angularDetInc = 0;
+  double xs1, ys1, xs2, ys2, xd1 = 0, yd1 = 0, xd2 = 0, yd2 = 0;
+  M3 inc;
+  std::vector<ViewPos> views;
+  ViewPos* d_views = nullptr;
+  size_t d_views_cap = 0;
+  float* d_sino = nullptr;
+  size_t d_sino_cap = 0;
+  ~ctgpu_scanner() {
+    if (d_views) cudaFree(d_views);
+    if (d_sino) cudaFree(d_sino);
+  }
+};
+
+struct ctgpu_recon {
+  ctgpu_geometry g;
+  int nx, ny, interp, bproj, interpFactor;
+  int iDetCenter, pitch;
+  double xMin, xMax, yMin, yMax, xInc, yInc, rotScale, startR, startPhi;
+  FilterDesign fd;
+  float* d_taps = nullptr;
+  float* d_weights = nullptr;
+  float* d_filtered = nullptr;
+  size_t d_filtered_cap = 0;
+  double* d_angles = nullptr;
+  size_t d_angles_cap = 0;
+  unsigned char* d_views = nullptr;
+  size_t d_views_cap = 0;
+  unsigned char* d_scratch = nullptr;
+  size_t d_scratch_cap = 0;
+  float* d_sino = nullptr;   // run_host staging
+  size_t d_sino_cap = 0;
+  float* d_image = nullptr;
+  size_t d_image_cap = 0;
+  ~ctgpu_recon() {
+    for (void* p : {(void*)d_taps, (void*)d_weights, (void*)d_filtered, (void*)d_angles,
+                    (void*)d_views, (void*)d_scratch, (void*)d_sino, (void*)d_image})
+      if (p) cudaFree(p);
+  }
+};
+
+extern "C" {
+
+const char* ctgpu_last_error(void) { return g_err.c_str(); }
+int ctgpu_abi_version(void) { return CTGPU_ABI_VERSION; }
+
+int ctgpu_sync(void* stream) {
+  CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  CUDA_TRY(cudaGetLastError());
+  unsigned int st = 0;
+  CUDA_TRY(status_read_and_clear(&st));
+  if (st & kStatusTimeout)
+    return fail(CTGPU_ERR_TIMEOUT, "a kernel's bounded shared-memory wait expired; output invalid");
+  if (st & kStatusFeatherRange)
+    return fail(CTGPU_ERR_INVALID, "HalfScanFeather: complementary view outside the half scan");
+  return ok();
+}
+
+// ---------------------------------------------------------------- phantom --
+int ctgpu_phantom_create(ctgpu_phantom** out) {
+  if (!out) return fail(CTGPU_ERR_INVALID, "null output pointer");
+  *out = new ctgpu_phantom();
+  return ok();
+}
+
+int ctgpu_phantom_add_element(ctgpu_phantom* p, const char* type, double cx, double cy, double u,
+                              double v, double rot_deg, double atten) {
+  if (!p || !type) return fail(CTGPU_ERR_INVALID, "null argument");
+  int t = elem_type(type);
+  if (!t) return fail(CTGPU_ERR_INVALID, std::string("Unknown PhantomElement type ") + type);
+  if (!(u > 0) || !(v > 0)) return fail(CTGPU_ERR_INVALID, "element sizes must be positive");
+  PElem e = make_elem(t, cx, cy, u, v, rot_deg, atten);
+  p->elems.insert(p->elems.begin(), e);   // std::list::push_front (phantom.cpp:247)
+  if (p->xmin > e.bx0) p->xmin = e.bx0;
+  if (p->xmax < e.bx1) p->xmax = e.bx1;
+  if (p->ymin > e.by0) p->ymin = e.by0;
+  if (p->ymax < e.by1) p->ymax = e.by1;
+  p->dirty = true;
+  return ok();
+}
+
+int ctgpu_phantom_create_builtin(const char* name, ctgpu_phantom** out) {
+  if (!name || !out) return fail(CTGPU_ERR_INVALID, "null argument");
+  static const double shepp[11][6] = {   // phantom.cpp:390-404
+      {0.0000, 0.0000, 0.6900, 0.9200, 0.0, 1.00},   {0.0000, -0.0184, 0.6624, 0.8740, 0.0, -0.98},
+      {0.2200, 0.0000, 0.1100, 0.3100, -18.0, -0.02}, {-0.2200, 0.0000, 0.1600, 0.4100, 18.0, -0.02},
+      {0.0000, 0.3500, 0.2100, 0.2500, 0.0, 0.01},    {0.0000, 0.1000, 0.0460, 0.0460, 0.0, 0.01},
+      {0.0000, -0.1000, 0.0460, 0.0460, 0.0, 0.01},   {-0.0800, -0.6050, 0.0460, 0.0230, 0.0, 0.01},
+      {0.0000, -0.6050, 0.0230, 0.0230, 0.0, 0.01},   {0.0600, -0.6050, 0.0230, 0.0230, 0.0, 0.01},
+      {0.5538, -0.3858, 0.0330, 0.2060, -18.0, 0.03}};
+  static const struct { const char* t; double a[6]; } herman[15] = {   // phantom.cpp:415-433
+      {"ellipse", {0.000, 1.50, 0.375, 0.3000, 90.00, -0.003}},
+      {"ellipse", {0.675, -0.75, 0.225, 0.1500, 140.00, 0.010}},
+      {"ellipse", {0.750, 1.50, 0.375, 0.2250, 50.00, 0.003}},
+      {"segment", {1.375, -7.50, 1.100, 0.6250, 19.20, -0.204}},
+      {"segment", {1.375, -7.50, 1.100, 4.3200, 19.21, 0.204}},
+      {"segment", {0.000, -2.25, 1.125, 0.3750, 0.00, -0.003}},
+      {"segment", {0.000, -2.25, 1.125, 3.0000, 0.00, 0.003}},
+      {"segment", {-1.000, 3.75, 1.000, 0.5000, 135.00, -0.003}},
+      {"segment", {-1.000, 3.75, 1.000, 3.0000, 135.00, 0.003}},
+      {"segment", {1.000, 3.75, 1.000, 0.5000, 225.00, -0.003}},
+      {"segment", {1.000, 3.75, 1.000, 3.0000, 225.00, 0.003}},
+      {"triangle", {5.025, 3.75, 1.125, 0.5000, 110.75, 0.206}},
+      {"triangle", {-5.025, 3.75, 1.125, 0.9000, -110.75, 0.206}},
+      {"ellipse", {0.000, 0.00, 8.625, 6.4687, 90.00, 0.416}},
+      {"ellipse", {0.000, 0.00, 7.875, 5.7187, 90.00, -0.206}}};
+  ctgpu_phantom* p = new ctgpu_phantom();
+  if (!strcasecmp(name, "shepp-logan")) {
+    for (auto& r : shepp) ctgpu_phantom_add_element(p, "ellipse", r[0], r[1], r[2], r[3], r[4], r[5]);
+  } else if (!strcasecmp(name, "herman")) {
+    for (auto& r : herman)
+      ctgpu_phantom_add_element(p, r.t, r.a[0], r.a[1], r.a[2], r.a[3], r.a[4], r.a[5]);
+  } else if (!strcasecmp(name, "unit-pulse")) {
+    p->unitPulse = true;
+    ctgpu_phantom_add_element(p, "rectangle", 0., 0., 100., 100., 0., 0.);
+    ctgpu_phantom_add_element(p, "ellipse", 0., 0., 1., 1., 0., 1.);
+  } else {
+    delete p;
+    return fail(CTGPU_ERR_INVALID, std::string("Invalid phantom name ") + name);
+  }
+  *out = p;
+  return ok();
+}
+
+int ctgpu_phantom_read_file(ctgpu_phantom* p, const char* filename) {
+  if (!p || !filename) return fail(CTGPU_ERR_INVALID, "null argument");
+  FILE* fp = std::fopen(filename, "r");
+  if (!fp) return fail(CTGPU_ERR_IO, std::string("cannot open phantom file ") + filename);
+  int rc = CTGPU_OK;
+  std::string bad;
+  while (true) {   // phantom.cpp:195-209
+    char type[80];
+    double cx, cy, u, v, rot, dens;
+    int st = std::fscanf(fp, "%79s %lf %lf %lf %lf %lf %lf", type, &cx, &cy, &u, &v, &rot, &dens);
+    if (st == EOF) break;
+    if (st != 7) { rc = CTGPU_ERR_INVALID; bad = "Insufficient fields reading phantom file"; break; }
+    int r = ctgpu_phantom_add_element(p, type, cx, cy, u, v, rot, dens);
+    if (r != CTGPU_OK) { rc = r; bad = g_err; break; }
+  }
+  std::fclose(fp);
+  return rc == CTGPU_OK ? ok() : fail(rc, bad);
+}
+
+int ctgpu_phantom_bounds(const ctgpu_phantom* p, double bounds[4], int* n_elements) {
+  if (!p) return fail(CTGPU_ERR_INVALID, "null phantom");
+  if (bounds) { bounds[0] = p->xmin; bounds[1] = p->xmax; bounds[2] = p->ymin; bounds[3] = p->ymax; }
+  if (n_elements) *n_elements = (int)p->elems.size();
+  return ok();
+}
+
+void ctgpu_phantom_destroy(ctgpu_phantom* p) { delete p; }
+
+// ---------------------------------------------------------------- scanner --
+int ctgpu_scanner_create(const ctgpu_phantom* p, const char* geometry_name, int nDet, int nView,
+                         int offsetView, int nSample, double rotAngle, double flRatio,
+                         double cdRatio, double viewRatio, double scanRatio, ctgpu_scanner** out) {
+  if (!p || !geometry_name || !out) return fail(CTGPU_ERR_INVALID, "null argument");
+  int geom = geometry_from_name(geometry_name);
+  if (geom < 0) return fail(CTGPU_ERR_INVALID, std::string("Invalid geometry name ") + geometry_name);
+  if (nView < 1 || nDet < 1) return fail(CTGPU_ERR_INVALID, "nView & nDet must be greater than 0");
+  if (nSample < 1) return fail(CTGPU_ERR_INVALID, "nSample must be greater than 0");
+  if (p->elems.empty()) return fail(CTGPU_ERR_INVALID, "phantom has no elements");
+  ctgpu_scanner* s = new ctgpu_scanner();
+  s->geometry = geom; s->nDet = nDet; s->nView = nView; s->offsetView = offsetView;
+  s->nSample = nSample;
+  // Scanner::Scanner (scanner.cpp:110-222)
+  double maxAxis = std::fmax(p->xmax - p->xmin, p->ymax - p->ymin);
+  maxAxis = (p->xmax - p->xmin) > (p->ymax - p->ymin) ? (p->xmax - p->xmin) : (p->ymax - p->ymin);
+  s->viewDiameter = kSqrt2 * maxAxis * viewRatio;
+  s->focalLength = (s->viewDiameter / 2) * flRatio;
+  s->centerDetectorLength = (s->viewDiameter / 2) * cdRatio;
+  s->sourceDetectorLength = s->focalLength + s->centerDetectorLength;
+  s->scanDiameter = s->viewDiameter * scanRatio;
+  s->xCenter = p->xmin + (p->xmax - p->xmin) / 2;
+  s->yCenter = p->ymin + (p->ymax - p->ymin) / 2;
+  s->rotLen = rotAngle;
+  s->rotInc = s->rotLen / nView;
+  bool even = (nDet % 2) == 0;
+  if (geom == kParallel) {
+    s->fanBeamAngle = 0;
+    s->detLen = s->scanDiameter;
+    s->detStart = -s->detLen / 2;
+    s->detInc = s->detLen / nDet;
+    double endOff = 0;
+    if (even) { s->detInc = s->detLen / (nDet - 1); endOff = s->detInc; }
+    double half = s->detLen / 2;
+    s->xs1 = s->xCenter - half; s->ys1 = s->yCenter + s->focalLength;
+    s->xs2 = s->xCenter + half + endOff; s->ys2 = s->yCenter + s->focalLength;
+    s->xd1 = s->xCenter - half; s->yd1 = s->yCenter - s->centerDetectorLength;
+    s->xd2 = s->xCenter + half + endOff; s->yd2 = s->yCenter - s->centerDetectorLength;
+    s->detLen += endOff;
+  } else if (geom == kEquilinear) {
+    if (s->scanDiameter / 2 >= s->focalLength) {
+      delete s;
+      return fail(CTGPU_ERR_INVALID, "Invalid geometry: Focal length must be larger than scan length");
+    }
+    double ang = std::asin((s->scanDiameter / 2) / s->focalLength);
+    double half = s->sourceDetectorLength * std::tan(ang);
+    s->detLen = half * 2;
+    s->detStart = -half;
+    s->detInc = s->detLen / nDet;
+    double endOff = 0;
+    if (even) { s->detInc = s->detLen / (nDet - 1); endOff = s->detInc; s->detLen += endOff; }
+    s->fanBeamAngle = ang * 2;
+    s->xs1 = s->xCenter; s->ys1 = s->yCenter + s->focalLength;
+    s->xs2 = s->xCenter; s->ys2 = s->yCenter + s->focalLength;
+    s->xd1 = s->xCenter - half; s->yd1 = s->yCenter - s->centerDetectorLength;
+    s->xd2 = s->xCenter + half + endOff; s->yd2 = s->yCenter - s->centerDetectorLength;
+  } else {
+    if (s->scanDiameter / 2 > s->focalLength) {
+      delete s;
+      return fail(CTGPU_ERR_INVALID, "Invalid geometry: Focal length must be larger than scan length");
+    }
+    double ang = std::asin((s->scanDiameter / 2) / s->focalLength);
+    s->detLen = 2 * ang;
+    s->detStart = -ang;
+    s->detInc = s->detLen / nDet;
+    double endOff = 0;
+    if (even) { s->detInc = s->detLen / (nDet - 1); endOff = s->detInc; }
+    double a1 = std::acos((s->scanDiameter / 2) / s->centerDetectorLength);
+    double angScale = 2 * (kHalfPi + ang - a1) / s->detLen;
+    s->angularDetLen = angScale * (s->detLen + endOff);
+    s->angularDetInc = angScale * s->detInc;
+    s->fanBeamAngle = ang * 2;
+    s->xs1 = s->xCenter; s->ys1 = s->yCenter + s->focalLength;
+    s->xs2 = s->xCenter; s->ys2 = s->yCenter + s->focalLength;
+    s->detLen += endOff;
+  }
+  s->inc = mul(mul(xlat(-s->xCenter, -s->yCenter), rotm(s->rotInc)), xlat(s->xCenter, s->yCenter));
+  *out = s;
+  return ok();
+}
+
+int ctgpu_scanner_geometry(const ctgpu_scanner* s, ctgpu_geometry* g) {
+  if (!s || !g) return fail(CTGPU_ERR_INVALID, "null argument");
+  std::memset(g, 0, sizeof(*g));   // Projections::initFromScanner (projections.cpp:145-161)
+  g->geometry = s->geometry;
+  g->n_det = s->nDet;
+  g->n_view = s->nView;
+  g->rot_start = s->offsetView * s->rotInc;
+  g->rot_inc = s->rotInc;
+  g->det_start = s->detStart;
+  g->det_inc = s->detInc;
+  g->view_diameter = s->viewDiameter;
+  g->focal_length = s->focalLength;
+  g->source_detector_length = s->sourceDetectorLength;
+  g->fan_beam_angle = s->fanBeamAngle;
+  return ok();
+}
+
+void ctgpu_scanner_destroy(ctgpu_scanner* s) { delete s; }
+
+// View end points by the reference's incremental rotation (scanner.cpp:301-417).
+static void scanner_views(ctgpu_scanner* s, int startView, int nViews, int offsetView) {
+  s->views.resize(nViews);
+  double start = (startView + offsetView) * s->rotInc;
+  M3 m0 = mul(mul(xlat(-s->xCenter, -s->yCenter), rotm(start)), xlat(s->xCenter, s->yCenter));
+  double xd1 = 0, yd1 = 0, xd2 = 0, yd2 = 0;
+  if (s->geometry != kEquiangular) {
+    xd1 = s->xd1; yd1 = s->yd1; xd2 = s->xd2; yd2 = s->yd2;
+    apply(m0, xd1, yd1);
+    apply(m0, xd2, yd2);
+  }
+  double xs1 = s->xs1, ys1 = s->ys1, xs2 = s->xs2, ys2 = s->ys2;
+  apply(m0, xs1, ys1);
+  apply(m0, xs2, ys2);
+  double ang = start;
+  for (int v = 0; v < nViews; v++, ang += s->rotInc) {
+    s->views[v] = ViewPos{xs1, ys1, xs2, ys2, xd1, yd1, xd2, yd2, ang};
+    apply(s->inc, xs1, ys1);
+    apply(s->inc, xs2, ys2);
+    if (s->geometry != kEquiangular) {
+      apply(s->inc, xd1, yd1);
+      apply(s->inc, xd2, yd2);
+    }
+  }
+}
+
+int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int startView,
+                              int nViews, int offsetView, int storageOffset, float* d_sino,
+                              int pitch, double* h_angles, void* stream) {
+  if (!s || !p || !d_sino) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (pitch < s->nDet) return fail(CTGPU_ERR_INVALID, "sinogram pitch smaller than nDet");
+  if (nViews < 0 || storageOffset < 0) return fail(CTGPU_ERR_INVALID, "negative view range");
+  if (nViews == 0) return ok();
+  cudaStream_t st = (cudaStream_t)stream;
+  scanner_views(s, startView, nViews, offsetView);
+  if (h_angles)
+    for (int v = 0; v < nViews; v++) h_angles[storageOffset + v] = s->views[v].angle;
+  if (p->unitPulse) {   // scanner.cpp:475-478
+    CUDA_TRY(launch_unit_pulse(d_sino, nViews, s->nDet, pitch, storageOffset, st));
+    return ok();
+  }
+  CUDA_TRY(const_cast<ctgpu_phantom*>(p)->upload(st));
+  CUDA_TRY(ensure_device(s->d_views, s->d_views_cap, (size_t)nViews));
+  CUDA_TRY(cudaMemcpyAsync(s->d_views, s->views.data(), sizeof(ViewPos) * nViews,
+                           cudaMemcpyHostToDevice, st));
+  RaysumLaunch L{};
+  L.geometry = s->geometry;
+  L.nDet = s->nDet;
+  L.nSample = s->nSample;
+  L.nElem = (int)p->elems.size();
+  L.nViews = nViews;
+  L.pitch = pitch;
+  L.rowOffset = storageOffset;
+  L.centerDetectorLength = s->centerDetectorLength;
+  L.angularDetLen = s->angularDetLen;
+  L.angularDetInc = s->angularDetInc;
+  L.elems = p->d_elems;
+  L.views = s->d_views;
+  L.sino = d_sino;
+  L.status = status_pointer();
+  cudaError_t e = launch_raysum(L, st);
+  if (e == cudaErrorInvalidValue)
+    return fail(CTGPU_ERR_UNSUPPORTED, "too many phantom elements x rays per detector for one CTA");
+  CUDA_TRY(e);
+  return ok();
+}
+
+int ctgpu_collect_projections_host(ctgpu_scanner* s, const ctgpu_phantom* p, int startView,
+                                   int nViews, int offsetView, int storageOffset, float* h_sino,
+                                   double* h_angles) {
+  if (!s || !p || !h_sino) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (storageOffset + nViews > s->nView) return fail(CTGPU_ERR_INVALID, "view range past nView");
+  int pitch = pitch_for(s->nDet);
+  CUDA_TRY(ensure_device(s->d_sino, s->d_sino_cap, (size_t)nViews * pitch));
+  int rc = ctgpu_collect_projections(s, p, startView, nViews, offsetView, 0, s->d_sino, pitch,
+                                     h_angles ? h_angles + storageOffset : nullptr, nullptr);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpy2D(h_sino + (size_t)storageOffset * s->nDet, sizeof(float) * s->nDet,
+                        s->d_sino, sizeof(float) * pitch, sizeof(float) * s->nDet, nViews,
+                        cudaMemcpyDeviceToHost));
+  return ctgpu_sync(nullptr);
+}
+
+// ---------------------------------------------------------- reconstruction --
+int ctgpu_recon_create(const ctgpu_geometry* g, int nx, int ny, const char* filterName,
+                       double filterParam, const char* filterMethod, int zeropad,
+                       const char* filterGeneration, const char* interpName, int interpFactor,
+                       const char* backprojName, const ctgpu_roi* roi, ctgpu_recon** out) {
+  if (!g || !out || !filterName || !filterMethod || !filterGeneration || !interpName ||
+      !backprojName)
+    return fail(CTGPU_ERR_INVALID, "null argument");
+  if (g->geometry < 0 || g->geometry > 2)
+    return fail(CTGPU_ERR_INVALID, "Unable to select a backprojection method [Backprojector::initBackprojector]");
+  if (nx < 1 || ny < 1 || g->n_det < 2 || g->n_view < 1)
+    return fail(CTGPU_ERR_INVALID, "image and scan sizes must be positive (nDet >= 2)");
+  int fid = filter_id_from_name(filterName);
+  int mid = filter_method_from_name(filterMethod);
+  int gid = filter_generation_from_name(filterGeneration);
+  // ProcessSignal ctor error order (procsignal.cpp:88-115)
+  if (mid < 0) return fail(CTGPU_ERR_INVALID, std::string("Error creating ProcessSignal: Invalid filter method name ") + filterMethod);
+  if (gid < 0) return fail(CTGPU_ERR_INVALID, std::string("Error creating ProcessSignal: Invalid frequency filter name ") + filterGeneration);
+  if (fid < 0) return fail(CTGPU_ERR_INVALID, std::string("Error creating ProcessSignal: Invalid Filter name ") + filterName);
+  int bp = backproj_from_name(backprojName);
+  int ip = interp_from_name(interpName);
+  if (bp < 0) return fail(CTGPU_ERR_INVALID, std::string("Error creating backprojector: Invalid backprojection name ") + backprojName);
+  if (ip < 0) return fail(CTGPU_ERR_INVALID, std::string("Error creating backprojector: Invalid interpolation name ") + interpName);
+  if (interpFactor < 1) return fail(CTGPU_ERR_INVALID, "interpolation factor must be >= 1");
+  FilterSpec sp{};
+  sp.filterId = fid; sp.method = mid; sp.generation = gid; sp.zeropad = zeropad;
+  sp.interpFactor = interpFactor; sp.geometry = g->geometry; sp.nDet = g->n_det;
+  sp.param = filterParam; sp.bandwidth = 1. / g->det_inc; sp.detInc = g->det_inc;
+  sp.focalLength = g->focal_length; sp.sdl = g->source_detector_length;
+  ctgpu_recon* r = new ctgpu_recon();
+  std::string err;
+  if (!design_filter(sp, r->fd, err)) {
+    delete r;
+    return fail(mid == 3 ? CTGPU_ERR_UNSUPPORTED : CTGPU_ERR_INVALID, err);
+  }
+  r->g = *g;
+  r->nx = nx; r->ny = ny; r->interp = ip;
+  r->bproj = (g->geometry == kParallel) ? bp : kTable;   // fan beams: table-derived classes (:160-163)
+  r->interpFactor = interpFactor;
+  r->iDetCenter = (g->n_det - 1) / 2;
+  r->pitch = pitch_for(g->n_det);
+  // Backproject::Backproject (backprojectors.cpp:264-319)
+  r->rotScale = g->geometry == kParallel ? kPi / g->n_view : (2 * kPi) / g->n_view;
+  double phmLen = g->view_diameter / kSqrt2;
+  r->xMin = -phmLen / 2; r->xMax = r->xMin + phmLen;
+  r->yMin = -phmLen / 2; r->yMax = r->yMin + phmLen;
+  if (roi) {
+    if (roi->x_min > r->xMin) r->xMin = roi->x_min;
+    if (roi->x_max < r->xMax) r->xMax = roi->x_max;
+    if (roi->y_min > r->yMin) r->yMin = roi->y_min;
+    if (roi->y_max < r->yMax) r->yMax = roi->y_max;
+    if (r->xMin > r->xMax) std::swap(r->xMin, r->xMax);
+    if (r->yMin > r->yMax) std::swap(r->yMin, r->yMax);
+  }
+  r->xInc = (r->xMax - r->xMin) / nx;
+  r->yInc = (r->yMax - r->yMin) / ny;
+  double x0 = r->xMin + r->xInc / 2, y0 = r->yMin + r->yInc / 2;
+  r->startR = std::sqrt(x0 * x0 + y0 * y0);
+  r->startPhi = std::atan2(y0, x0);
+  size_t nt = r->fd.taps.size(), nw = r->fd.weights.size(), c1 = 0, c2 = 0;
+  cudaError_t e = ensure_device(r->d_taps, c1, nt);
+  if (e == cudaSuccess) e = ensure_device(r->d_weights, c2, nw);
+  if (e == cudaSuccess) e = cudaMemcpy(r->d_taps, r->fd.taps.data(), sizeof(float) * nt, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(r->d_weights, r->fd.weights.data(), sizeof(float) * nw, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    delete r;
+    return fail(CTGPU_ERR_CUDA, std::string("recon_create: ") + cudaGetErrorString(e));
+  }
+  *out = r;
+  return ok();
+}
+
+int ctgpu_recon_image_axes(const ctgpu_recon* r, double extent[4], double increment[2]) {
+  if (!r) return fail(CTGPU_ERR_INVALID, "null plan");
+  if (extent) { extent[0] = r->xMin; extent[1] = r->xMax; extent[2] = r->yMin; extent[3] = r->yMax; }
+  if (increment) { increment[0] = r->xInc; increment[1] = r->yInc; }
+  return ok();
+}
+
+void ctgpu_recon_destroy(ctgpu_recon* r) { delete r; }
+
+int ctgpu_recon_filter(ctgpu_recon* r, const float* d_sino, int sinoPitch, int nViews,
+                       float* d_filtered, int filtPitch, void* stream) {
+  if (!r || !d_sino || !d_filtered) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (sinoPitch < r->g.n_det || filtPitch < r->g.n_det) return fail(CTGPU_ERR_INVALID, "pitch < nDet");
+  FilterLaunch L{};
+  L.nDet = r->g.n_det;
+  L.nViews = nViews;
+  L.inPitch = sinoPitch;
+  L.outPitch = filtPitch;
+  L.taps = r->d_taps;
+  L.weights = r->d_weights;
+  L.in = d_sino;
+  L.out = d_filtered;
+  cudaError_t e = launch_filter(L, (cudaStream_t)stream);
+  if (e == cudaErrorInvalidValue) return fail(CTGPU_ERR_UNSUPPORTED, "nDet too large for the shared-memory filter");
+  CUDA_TRY(e);
+  return ok();
+}
+
+// Backprojection of nViews filtered rows; outScale multiplies this launch's sum.
+static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int pitch,
+                                    const double* h_angles, int nViews, float* d_image,
+                                    int accumulate, float outScale, cudaStream_t st) {
+  if (nViews <= 0) {
+    if (!accumulate) CUDA_TRY(cudaMemsetAsync(d_image, 0, sizeof(float) * r->nx * r->ny, st));
+    return ok();
+  }
+  CUDA_TRY(ensure_device(r->d_angles, r->d_angles_cap, (size_t)nViews));
+  CUDA_TRY(cudaMemcpyAsync(r->d_angles, h_angles, sizeof(double) * nViews, cudaMemcpyHostToDevice, st));
+  const void* views = nullptr;
+  if (r->bproj == kIDiff || r->bproj == kDiff) {
+    // per-view steps in the reference's own FP64 / fixed-point arithmetic
+    // (backprojectors.cpp:522-527 diff, :593-597 idiff)
+    std::vector<long long> iv;
+    std::vector<double> dv;
+    const double scale = 4294967296.0;
+    for (int v = 0; v < nViews; v++) {
+      double th = h_angles[v];
+      if (r->bproj == kIDiff) {
+        iv.push_back(nearest_ll(r->xInc * std::cos(th) / r->g.det_inc * scale));
+        iv.push_back(nearest_ll(r->yInc * std::sin(th) / r->g.det_inc * scale));
+        iv.push_back(nearest_ll((r->startR * std::cos(th - r->startPhi) / r->g.det_inc + r->iDetCenter) * scale));
+      } else {
+        dv.push_back(r->xInc * std::cos(th) / r->g.det_inc);
+        dv.push_back(r->yInc * std::sin(th) / r->g.det_inc);
+        dv.push_back(r->iDetCenter + r->startR * std::cos(th - r->startPhi) / r->g.det_inc);
+      }
+    }
+    size_t bytes = 24 * (size_t)nViews;
+    CUDA_TRY(ensure_device(r->d_views, r->d_views_cap, bytes));
+    CUDA_TRY(cudaMemcpyAsync(r->d_views, r->bproj == kIDiff ? (const void*)iv.data() : (const void*)dv.data(),
+                             bytes, cudaMemcpyHostToDevice, st));
+    views = r->d_views;
+  }
+  size_t sb = backproject_scratch_bytes(r->bproj, nViews, r->nx);
+  if (sb) CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
+  BackprojLaunch L{};
+  L.geometry = r->g.geometry;
+  L.interp = r->interp;
+  L.bproj = r->bproj;
+  L.nDet = r->g.n_det;
+  L.nx = r->nx;
+  L.ny = r->ny;
+  L.nViews = nViews;
+  L.pitch = pitch;
+  L.iDetCenter = r->iDetCenter;
+  L.detInc = r->g.det_inc;
+  L.xMin = r->xMin;
+  L.yMin = r->yMin;
+  L.xInc = r->xInc;
+  L.yInc = r->yInc;
+  L.focalLength = r->g.focal_length;
+  L.sdl = r->g.source_detector_length;
+  L.rotScale = r->rotScale;
+  L.angles = r->d_angles;
+  L.filtered = d_filtered;
+  L.image = d_image;
+  L.accumulate = accumulate;
+  L.outScale = outScale;
+  L.status = status_pointer();
+  cudaError_t e = launch_backproject_views(L, views, r->d_scratch, st);
+  if (e == cudaErrorInvalidValue)
+    return fail(CTGPU_ERR_UNSUPPORTED, "image pixels behind the fan-beam source");
+  CUDA_TRY(e);
+  return ok();
+}
+
+static float raw_scale(const ctgpu_recon* r) {
+  double s = 1.0;
+  if (r->bproj == kTrig) s *= r->rotScale;   // per-update rotScale (backprojectors.cpp:386-397)
+  if (r->g.geometry == kEquilinear) s *= r->g.focal_length * r->g.focal_length;   // 1/U^2 = FL^2/vy^2
+  return (float)s;
+}
+
+int ctgpu_recon_backproject(ctgpu_recon* r, const float* d_filtered, int pitch,
+                            const double* h_angles, int nViews, float* d_image, int accumulate,
+                            void* stream) {
+  if (!r || !d_filtered || !h_angles || !d_image) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (pitch < r->g.n_det || (pitch & 3)) return fail(CTGPU_ERR_INVALID, "filtered pitch must be >= nDet and a multiple of 4");
+  if (((uintptr_t)d_filtered & 15) != 0) return fail(CTGPU_ERR_INVALID, "filtered rows must be 16-byte aligned");
+  return recon_backproject_scaled(r, d_filtered, pitch, h_angles, nViews, d_image, accumulate,
+                                  raw_scale(r), (cudaStream_t)stream);
+}
+
+int ctgpu_recon_postprocess(ctgpu_recon* r, float* d_image, void* stream) {
+  if (!r || !d_image) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (r->bproj == kTrig) return ok();   // trig scales per update (Backproject::PostProcessing)
+  CUDA_TRY(launch_scale_image(d_image, (size_t)r->nx * r->ny, (float)r->rotScale, (cudaStream_t)stream));
+  return ok();
+}
+
+int ctgpu_recon_run(ctgpu_recon* r, const float* d_sino, int sinoPitch, const double* h_angles,
+                    int startView, int nViews, float* d_image, int flags, void* stream) {
+  if (!r || !d_sino || !h_angles || !d_image) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (nViews <= 0) nViews = r->g.n_view - startView;   // reconstructView(start, -1)
+  if (startView < 0 || startView + nViews > r->g.n_view) return fail(CTGPU_ERR_INVALID, "view range outside the projections");
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(ensure_device(r->d_filtered, r->d_filtered_cap, (size_t)nViews * r->pitch));
+  int rc = ctgpu_recon_filter(r, d_sino + (size_t)startView * sinoPitch, sinoPitch, nViews,
+                              r->d_filtered, r->pitch, stream);
+  if (rc) return rc;
+  bool acc = (flags & CTGPU_RUN_ACCUMULATE) != 0;
+  bool post = (flags & CTGPU_RUN_POSTPROCESS) != 0;
+  float scale = raw_scale(r);
+  if (post && !acc && r->bproj != kTrig) scale = (float)(scale * r->rotScale);   // fused PostProcessing
+  rc = recon_backproject_scaled(r, r->d_filtered, r->pitch, h_angles + startView, nViews, d_image,
+                                acc ? 1 : 0, scale, st);
+  if (rc) return rc;
+  if (post && acc) return ctgpu_recon_postprocess(r, d_image, stream);
+  return ok();
+}
+
+int ctgpu_recon_run_host(ctgpu_recon* r, const float* h_sino, const double* h_angles,
+                         float* h_image) {
+  if (!r || !h_sino || !h_angles || !h_image) return fail(CTGPU_ERR_INVALID, "null argument");
+  const int nDet = r->g.n_det, nView = r->g.n_view;
+  CUDA_TRY(ensure_device(r->d_sino, r->d_sino_cap, (size_t)nView * r->pitch));
+  CUDA_TRY(ensure_device(r->d_image, r->d_image_cap, (size_t)r->nx * r->ny));
+  CUDA_TRY(cudaMemcpy2D(r->d_sino, sizeof(float) * r->pitch, h_sino, sizeof(float) * nDet,
+                        sizeof(float) * nDet, nView, cudaMemcpyHostToDevice));
+  int rc = ctgpu_recon_run(r, r->d_sino, r->pitch, h_angles, 0, nView, r->d_image,
+                           CTGPU_RUN_POSTPROCESS, nullptr);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpy(h_image, r->d_image, sizeof(float) * r->nx * r->ny, cudaMemcpyDeviceToHost));
+  return ctgpu_sync(nullptr);
+}
+
+int ctgpu_recon_project(ctgpu_recon* r, const float* d_image, const double* h_angles, int nViews,
+                        float* d_sino, int pitch, float scale, void* stream) {
+  if (!r || !d_image || !h_angles || !d_sino) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (r->g.geometry != kParallel || r->interp != kLinear || r->bproj != kTable)
+    return fail(CTGPU_ERR_UNSUPPORTED, "projector: parallel geometry, table backprojector, linear interpolation");
+  if (pitch < r->g.n_det) return fail(CTGPU_ERR_INVALID, "pitch < nDet");
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(ensure_device(r->d_angles, r->d_angles_cap, (size_t)nViews));
+  CUDA_TRY(cudaMemcpyAsync(r->d_angles, h_angles, sizeof(double) * nViews, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemset2DAsync(d_sino, sizeof(float) * pitch, 0, sizeof(float) * r->g.n_det, nViews, st));
+  BackprojLaunch L{};
+  L.geometry = kParallel;
+  L.interp = kLinear;
+  L.bproj = kTable;
+  L.nDet = r->g.n_det;
+  L.nx = r->nx;
+  L.ny = r->ny;
+  L.nViews = nViews;
+  L.pitch = pitch;
+  L.iDetCenter = r->iDetCenter;
+  L.detInc = r->g.det_inc;
+  L.xMin = r->xMin;
+  L.yMin = r->yMin;
+  L.xInc = r->xInc;
+  L.yInc = r->yInc;
+  L.angles = r->d_angles;
+  L.status = status_pointer();
+  CUDA_TRY(launch_project_table(L, d_image, d_sino, scale, st));
+  return ok();
+}
+
+// ----------------------------------------------------------------- helical --
+static int helical_check(const ctgpu_geometry* g, int nViewIn, int interpView, int* last,
+                         int* offset) {
+  if (!g) return fail(CTGPU_ERR_INVALID, "null geometry");
+  if (g->geometry != kEquiangular) {   // projections.cpp:203-229
+    if (g->geometry == kParallel) return fail(CTGPU_ERR_INVALID, "Helical 180LI not yet implemented for PARALLEL geometry");
+    if (g->geometry == kEquilinear) return fail(CTGPU_ERR_INVALID, "Helical 180LI not yet implemented for EQUILINEAR geometry");
+    return fail(CTGPU_ERR_INVALID, "Invalid geometry in projection data file");
+  }
+  double dbeta = g->rot_inc, fan = g->fan_beam_angle;
+  if (nViewIn < (int)((2 * (kPi + fan)) / dbeta) - 1)
+    return fail(CTGPU_ERR_INVALID, "Data set does not include 360 +2*FanBeamAngle views");
+  *offset = 0;
+  if (interpView >= 0) {
+    if (interpView * dbeta < kPi + fan || interpView * dbeta + kPi + fan > nViewIn * dbeta)
+      return fail(CTGPU_ERR_INVALID, "There isn't PI+fanAngle of data on either side of the requested interpolation view");
+    *offset = interpView - (int)((kPi + fan) / dbeta);
+  }
+  *last = (int)((kPi + fan) / dbeta);
+  if (*offset + 2 * *last >= nViewIn)
+    return fail(CTGPU_ERR_INVALID, "Data set does not include 360 +2*FanBeamAngle views");
+  return ok();
+}
+
+int ctgpu_helical180li_size(const ctgpu_geometry* g, int nViewIn, int interpView, int* nOut) {
+  int last, off;
+  int rc = helical_check(g, nViewIn, interpView, &last, &off);
+  if (rc) return rc;
+  if (nOut) *nOut = last + 1;
+  return ok();
+}
+
+int ctgpu_helical180li(const ctgpu_geometry* g, const float* d_in, int nViewIn, int interpView,
+                       float* d_out, int pitch, double* h_angles, int* nOut, void* stream) {
+  int last, off;
+  int rc = helical_check(g, nViewIn, interpView, &last, &off);
+  if (rc) return rc;
+  if (!d_in || !d_out || pitch < g->n_det) return fail(CTGPU_ERR_INVALID, "bad buffers");
+  HelicalLaunch L{};
+  L.nDet = g->n_det;
+  L.nViewIn = nViewIn;
+  L.nViewOut = last + 1;
+  L.offsetView = off;
+  L.pitch = pitch;
+  L.dbeta = g->rot_inc;
+  L.dgamma = g->det_inc;
+  L.fan = g->fan_beam_angle;
+  L.in = d_in;
+  L.out = d_out;
+  L.status = status_pointer();
+  CUDA_TRY(launch_helical180li(L, (cudaStream_t)stream));
+  if (h_angles)
+    for (int i = 0; i <= last; i++) h_angles[i] = (i + off) * g->rot_inc;
+  if (nOut) *nOut = last + 1;
+  return ok();
+}
+
+int ctgpu_halfscan_feather(const ctgpu_geometry* g, float* d_data, int nView, int pitch,
+                           void* stream) {
+  if (!g || !d_data) return fail(CTGPU_ERR_INVALID, "null argument");
+  double dbeta = g->rot_inc, fan = g->fan_beam_angle;
+  if (nView != (int)((kPi + fan) / dbeta) + 1)   // projections.cpp:377-389
+    return fail(CTGPU_ERR_INVALID, "Data set does seem have enough data to be a halfscan data set");
+  if (g->geometry == kParallel) return fail(CTGPU_ERR_INVALID, "HalfScanFeather not yet implemented for PARALLEL geometry");
+  if (g->geometry != kEquiangular && g->geometry != kEquilinear) return fail(CTGPU_ERR_INVALID, "Invalid geometry");
+  cudaStream_t st = (cudaStream_t)stream;
+  float* tmp = nullptr;
+  size_t bytes = sizeof(float) * (size_t)nView * pitch;
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&tmp), bytes, st));
+  cudaError_t e = cudaMemcpyAsync(tmp, d_data, bytes, cudaMemcpyDeviceToDevice, st);
+  HelicalLaunch L{};
+  L.nDet = g->n_det;
+  L.nViewIn = nView;
+  L.nViewOut = nView;
+  L.pitch = pitch;
+  L.dbeta = dbeta;
+  L.dgamma = g->det_inc;
+  L.fan = fan;
+  L.in = tmp;
+  L.out = d_data;
+  L.status = status_pointer();
+  if (e == cudaSuccess) e = launch_halfscan_feather(L, st);
+  cudaFreeAsync(tmp, st);
+  CUDA_TRY(e);
+  return ok();
+}
+
+}  // extern "C"

@@ -1,0 +1,97 @@
+// ctgpu_internal.h -- structures shared by the host core and the sm_103a kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ctgpu {
+
+// ----- constants of the reference (include/ctsupport.h:167-179) -----------
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kHalfPi = 1.57079632679489661923;
+constexpr double kTwoPi = 6.28318530717958647692;
+constexpr double kSqrt2 = 1.414213562373095049;
+
+enum ElemType { kRect = 1, kTriangle = 2, kEllipse = 3, kSector = 4, kSegment = 5 };
+enum Geometry { kParallel = 0, kEquiangular = 1, kEquilinear = 2 };
+enum Interp { kNearest = 0, kLinear = 1, kCubic = 2 };
+enum Backproj { kTrig = 0, kTable = 1, kDiff = 2, kIDiff = 3 };
+
+// One phantom element, FP64 (PhantomElement, libctsim/phantom.cpp:554-566).
+struct PElem {
+  int type;
+  int pad;
+  double cx, cy, u, v, rot, atten;
+  double cosr, sinr;
+  double bx0, by0, bx1, by1;   // outline-polygon bounding box
+};
+
+// Source / detector end points of one view after the reference's incremental
+// rotation (libctsim/scanner.cpp:301-417), and its view angle.
+struct ViewPos {
+  double xs1, ys1, xs2, ys2, xd1, yd1, xd2, yd2, angle;
+};
+
+struct RaysumLaunch {
+  int geometry, nDet, nSample, nElem, nViews, pitch, rowOffset;
+  double centerDetectorLength, angularDetLen, angularDetInc;
+  const PElem* elems;
+  const ViewPos* views;
+  float* sino;
+  unsigned int* status;
+};
+
+// Filter: out[v][n] = sum_i (w[i] * in[v][i]) * taps[n - i + nDet - 1]
+struct FilterLaunch {
+  int nDet, nViews, inPitch, outPitch;
+  const float* taps;      // 2*nDet - 1
+  const float* weights;   // nDet (fan pre-weighting, 1 for parallel)
+  const float* in;
+  float* out;
+};
+
+// Backprojection of one problem.
+struct BackprojLaunch {
+  int geometry, interp, bproj;
+  int nDet, nx, ny, nViews, pitch;
+  int iDetCenter;
+  double detInc, xMin, yMin, xInc, yInc, focalLength, sdl, rotScale;
+  const double* angles;   // device, nViews
+  const float* filtered;  // device, [nViews][pitch]
+  float* image;           // device, [nx][ny]
+  int accumulate;         // add into image instead of overwriting
+  float outScale;         // applied to this launch's contribution (rotScale for trig)
+  unsigned int* status;
+};
+
+struct HelicalLaunch {
+  int nDet, nViewIn, nViewOut, offsetView, pitch;
+  double dbeta, dgamma, fan;
+  const float* in;    // original data
+  float* out;
+  unsigned int* status;
+};
+constexpr unsigned int kStatusFeatherRange = 2u;
+
+// status bits written by kernels
+constexpr unsigned int kStatusTimeout = 1u;
+
+// device status word (k_common.cu)
+unsigned int* status_pointer();
+cudaError_t status_read_and_clear(unsigned int* value);
+
+// kernel entry wrappers (defined in the .cu files)
+cudaError_t launch_raysum(const RaysumLaunch& L, cudaStream_t s);
+cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int rowOffset,
+                              cudaStream_t s);
+cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
+size_t backproject_scratch_bytes(int bproj, int nViews, int nx);
+cudaError_t launch_backproject_views(const BackprojLaunch& L, const void* views, void* scratch,
+                                     cudaStream_t s);
+cudaError_t launch_scale_image(float* image, size_t n, float scale, cudaStream_t s);
+cudaError_t launch_project_table(const BackprojLaunch& L, const float* image, float* sino,
+                                 float scale, cudaStream_t s);
+cudaError_t launch_helical180li(const HelicalLaunch& L, cudaStream_t s);
+cudaError_t launch_halfscan_feather(const HelicalLaunch& L, cudaStream_t s);
+
+}  // namespace ctgpu

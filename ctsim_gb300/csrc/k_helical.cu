@@ -1,0 +1,132 @@
+// k_helical.cu -- helical 180-degree linear interpolation and half-scan
+// feathering on sm_103a (Projections::Helical180LI_Equiangular and
+// Projections::HalfScanFeather, libctsim/projections.cpp:231-439).
+//
+// The reference scatters every input ray into the output view set with FP64
+// weights and accumulates in FP32 in view order.  Each output sample receives
+// at most two rays: its own (views before pi+fan) and its complementary ray
+// (detector mirrored, view shifted by 2*gamma - pi).  The kernels here gather
+// instead of scatter: one thread per output sample finds both source rays,
+// evaluates the same FP64 region tests and weights, and adds them in the
+// reference's order with the reference's FP32 rounding, so the result is
+// bit-identical and deterministic.
+#include "ctgpu_internal.h"
+
+namespace ctgpu {
+
+namespace {
+
+__device__ __forceinline__ int nearest_int(double x) { return x > 0 ? (int)(x + 0.5) : (int)(x - 0.5); }
+
+// weight of input ray (iv, id) in the 180LI sum; false outside regions 2-7
+// (projections.cpp:306-350)
+__device__ bool li_weight(double beta, double gamma, double fan, double* w) {
+  const double PI = kPi;
+  if (!((beta > fan - 2 * gamma) && (beta < 2 * PI + fan - 2 * gamma))) return false;
+  if (beta > fan - 2 * gamma && beta <= 2 * fan) *w = (beta + 2 * gamma - fan) / (PI + 2 * gamma);
+  else if (beta > 2 * fan && beta <= PI - 2 * gamma) *w = (beta + 2 * gamma - fan) / (PI + 2 * gamma);
+  else if (beta > PI - 2 * gamma && beta <= PI + fan) *w = (beta + 2 * gamma - fan) / (PI + 2 * gamma);
+  else if (beta > PI + fan && beta <= PI + 2 * fan - 2 * gamma) *w = (2 * PI - beta - 2 * gamma + fan) / (PI - 2 * gamma);
+  else if (beta > PI + 2 * fan - 2 * gamma && beta <= 2 * PI) *w = (2 * PI - beta - 2 * gamma + fan) / (PI - 2 * gamma);
+  else if (beta > 2 * PI && beta <= 2 * PI + fan - 2 * gamma) *w = (2 * PI - beta - 2 * gamma + fan) / (PI - 2 * gamma);
+  else return false;
+  return true;
+}
+
+}  // namespace
+
+__global__ void helical180li_kernel(HelicalLaunch L) {
+  const int vo = blockIdx.x;                  // output view
+  const int nDet = L.nDet;
+  const double dbeta = L.dbeta, dgamma = L.dgamma, fan = L.fan, PI = kPi;
+  const int last = L.nViewOut - 1, lastAcq = 2 * last;
+  for (int dO = threadIdx.x; dO < nDet; dO += blockDim.x) {
+    float o = 0.f;
+    // own ray: iv = vo, id = dO, valid while beta < pi + fan
+    {
+      int iv = vo, id = dO;
+      double beta = iv * dbeta;
+      double gamma = (id - (nDet - 1) / 2) * dgamma;
+      double w;
+      if (beta < PI + fan && li_weight(beta, gamma, fan, &w))
+        o = (float)((double)o + w * (double)L.in[(size_t)(iv + L.offsetView) * L.pitch + id]);
+    }
+    // complementary ray: id = nDet-1-dO, nearest(iv + (2 gamma - pi)/dbeta) == vo
+    {
+      int id = nDet - 1 - dO;
+      double gamma = (id - (nDet - 1) / 2) * dgamma;
+      int guess = (int)floor(vo - (2 * (id - (nDet - 1) / 2) * dgamma - PI) / dbeta);
+      for (int iv = guess - 2; iv <= guess + 2; iv++) {
+        if (iv < 0 || iv > lastAcq) continue;
+        double beta = iv * dbeta;
+        if (beta < PI + fan) continue;
+        int nv = nearest_int(((iv * dbeta) + 2 * (id - (nDet - 1) / 2) * dgamma - PI) / dbeta);
+        if (nv != vo) continue;
+        double w;
+        if (li_weight(beta, gamma, fan, &w))
+          o = (float)((double)o + w * (double)L.in[(size_t)(iv + L.offsetView) * L.pitch + id]);
+      }
+    }
+    L.out[(size_t)vo * L.pitch + dO] = o;
+  }
+}
+
+// feather weight w1 of the complementary sample at (beta1, gamma1)
+// (projections.cpp:408-421); false for the reference's "Shouldn't be here" case
+__device__ bool feather_w1(double beta1, double gamma1, double fan, double* w1) {
+  const double PI = kPi;
+  double x;
+  if (beta1 <= (fan - 2 * gamma1)) x = beta1 / (fan - 2 * gamma1);
+  else if ((fan - 2 * gamma1 <= beta1) && beta1 <= PI - 2 * gamma1) x = 1;
+  else if ((PI - 2 * gamma1 <= beta1) && (beta1 <= PI + fan)) x = (PI + fan - beta1) / (fan + 2 * gamma1);
+  else return false;
+  *w1 = (3 * x - 2 * x * x) * x;
+  return true;
+}
+
+__global__ void halfscan_feather_kernel(HelicalLaunch L) {
+  const int v = blockIdx.x;
+  const int nDet = L.nDet, nView = L.nViewOut;
+  const double dbeta = L.dbeta, dgamma = L.dgamma, fan = L.fan, PI = kPi;
+  const double sf = nView * L.dbeta / PI;
+  for (int d = threadIdx.x; d < nDet; d += blockDim.x) {
+    float x = L.in[(size_t)v * L.pitch + d];
+    double beta = v * dbeta;
+    double gamma = (d - (nDet - 1) / 2) * dgamma;
+    if (beta >= PI - 2 * gamma) {
+      // redundant sample: keeps weight w2 = 1 - w1 of its complement
+      int iv1 = nearest_int(((v * dbeta) + 2 * (d - (nDet - 1) / 2) * dgamma - PI) / dbeta);
+      double w1;
+      if (!feather_w1(iv1 * dbeta, -gamma, fan, &w1)) { atomicOr(L.status, kStatusFeatherRange); w1 = 0; }
+      x = (float)((double)x * (1 - w1));
+    } else {
+      // complement target of the redundant sample (iv2, nDet-1-d), if any
+      int id2 = nDet - 1 - d;
+      double gamma2 = (id2 - (nDet - 1) / 2) * dgamma;
+      int guess = (int)floor(v + (PI - 2 * gamma2) / dbeta);
+      for (int iv2 = guess - 2; iv2 <= guess + 2; iv2++) {
+        if (iv2 < 0 || iv2 >= nView) continue;
+        double beta2 = iv2 * dbeta;
+        if (!(beta2 >= PI - 2 * gamma2)) continue;
+        int iv1 = nearest_int(((iv2 * dbeta) + 2 * (id2 - (nDet - 1) / 2) * dgamma - PI) / dbeta);
+        if (iv1 != v) continue;
+        double w1;
+        if (!feather_w1(v * dbeta, -gamma2, fan, &w1)) { atomicOr(L.status, kStatusFeatherRange); w1 = 0; }
+        float x2 = L.in[(size_t)iv2 * L.pitch + id2];
+        x = (float)((double)x2 * w1);
+      }
+    }
+    L.out[(size_t)v * L.pitch + d] = (float)((double)x * sf);
+  }
+}
+
+cudaError_t launch_helical180li(const HelicalLaunch& L, cudaStream_t s) {
+  helical180li_kernel<<<L.nViewOut, 128, 0, s>>>(L);
+  return cudaGetLastError();
+}
+cudaError_t launch_halfscan_feather(const HelicalLaunch& L, cudaStream_t s) {
+  halfscan_feather_kernel<<<L.nViewOut, 128, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+}  // namespace ctgpu

@@ -1,0 +1,169 @@
+"""Device-resident entry points on torch CUDA tensors.
+
+torch supplies device memory and the current stream; every operation is a
+call through the C ABI into libctgpu.so's kernels.  Sinograms are
+[views, pitch] float32 with pitch a multiple of 4 (``alloc_sinogram``);
+images are [nx, ny] float32 (column-major v[ix][iy], as CTSim's ImageFile).
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._lib import Geometry, Roi, RUN_ACCUMULATE, RUN_POSTPROCESS, check, enc, lib
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def stream_handle(stream=None):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _ptr(t):
+    if not t.is_cuda or not t.is_contiguous() or t.dtype != _torch().float32:
+        raise ValueError("expected a contiguous float32 CUDA tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def pitch_for(n_det):
+    return (n_det + 3) & ~3
+
+
+def alloc_sinogram(n_view, n_det, device="cuda"):
+    torch = _torch()
+    return torch.zeros((n_view, pitch_for(n_det)), dtype=torch.float32, device=device)
+
+
+def raysums(scanner, phantom, sino, start_view=0, n_views=None, offset_view=None,
+            storage_offset=None, stream=None):
+    """Scanner::collectProjections into a device sinogram; returns the view angles."""
+    g = scanner.geometry()
+    nv = g.n_view - start_view if n_views is None else n_views
+    off = scanner.offsetView if offset_view is None else offset_view
+    store = start_view if storage_offset is None else storage_offset
+    ang = np.zeros(max(g.n_view, store + nv), np.float64)
+    check(lib().ctgpu_collect_projections(scanner._h, phantom._h, start_view, nv, off, store,
+                                          _ptr(sino), sino.shape[1],
+                                          ang.ctypes.data_as(C.c_void_p), stream_handle(stream)))
+    return ang
+
+
+class ReconPlan:
+    """A Reconstructor for device tensors (ctgpu_recon)."""
+
+    def __init__(self, geometry, nx, ny, filter_name="abs_bandlimit", filter_param=-1.0,
+                 filter_method="convolution", zeropad=1, filter_generation="direct",
+                 interp="linear", interp_factor=1, backproj="idiff", roi=None):
+        self.geometry = geometry
+        self.nx, self.ny = nx, ny
+        r = None if roi is None else Roi(*roi)
+        self._h = C.c_void_p()
+        check(lib().ctgpu_recon_create(C.byref(geometry), nx, ny, enc(filter_name), filter_param,
+                                       enc(filter_method), zeropad, enc(filter_generation),
+                                       enc(interp), interp_factor, enc(backproj),
+                                       C.byref(r) if r else None, C.byref(self._h)))
+
+    def axes(self):
+        ext = (C.c_double * 4)()
+        inc = (C.c_double * 2)()
+        check(lib().ctgpu_recon_image_axes(self._h, ext, inc))
+        return tuple(ext), tuple(inc)
+
+    def filter(self, sino, out, n_views=None, stream=None):
+        nv = sino.shape[0] if n_views is None else n_views
+        check(lib().ctgpu_recon_filter(self._h, _ptr(sino), sino.shape[1], nv, _ptr(out),
+                                       out.shape[1], stream_handle(stream)))
+        return out
+
+    def backproject(self, filtered, angles, image, accumulate=False, stream=None):
+        ang = np.ascontiguousarray(angles, np.float64)
+        check(lib().ctgpu_recon_backproject(self._h, _ptr(filtered), filtered.shape[1],
+                                            ang.ctypes.data_as(C.c_void_p), len(ang),
+                                            _ptr(image), int(accumulate), stream_handle(stream)))
+        return image
+
+    def postprocess(self, image, stream=None):
+        check(lib().ctgpu_recon_postprocess(self._h, _ptr(image), stream_handle(stream)))
+        return image
+
+    def run(self, sino, angles, image, start_view=0, n_views=-1, postprocess=True,
+            accumulate=False, stream=None):
+        ang = np.ascontiguousarray(angles, np.float64)
+        flags = (RUN_POSTPROCESS if postprocess else 0) | (RUN_ACCUMULATE if accumulate else 0)
+        check(lib().ctgpu_recon_run(self._h, _ptr(sino), sino.shape[1],
+                                    ang.ctypes.data_as(C.c_void_p), start_view, n_views,
+                                    _ptr(image), flags, stream_handle(stream)))
+        return image
+
+    def run_host(self, sino, angles):
+        """reconstructAllViews with host numpy buffers (copies inside the call)."""
+        s = np.ascontiguousarray(sino, np.float32)
+        a = np.ascontiguousarray(angles, np.float64)
+        out = np.zeros((self.nx, self.ny), np.float32)
+        check(lib().ctgpu_recon_run_host(self._h, s.ctypes.data_as(C.c_void_p),
+                                         a.ctypes.data_as(C.c_void_p),
+                                         out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def project(self, image, angles, out, scale=1.0, stream=None):
+        ang = np.ascontiguousarray(angles, np.float64)
+        check(lib().ctgpu_recon_project(self._h, _ptr(image), ang.ctypes.data_as(C.c_void_p),
+                                        len(ang), _ptr(out), out.shape[1], float(scale),
+                                        stream_handle(stream)))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().ctgpu_recon_destroy(self._h)
+            self._h = None
+
+
+def helical180li(geometry, sino, interp_view=-1, stream=None):
+    """Projections::Helical180LI on a device sinogram; returns (out, angles)."""
+    torch = _torch()
+    n = C.c_int()
+    check(lib().ctgpu_helical180li_size(C.byref(geometry), sino.shape[0], interp_view, C.byref(n)))
+    out = torch.empty((n.value, sino.shape[1]), dtype=torch.float32, device=sino.device)
+    ang = np.zeros(n.value, np.float64)
+    check(lib().ctgpu_helical180li(C.byref(geometry), _ptr(sino), sino.shape[0], interp_view,
+                                   _ptr(out), sino.shape[1], ang.ctypes.data_as(C.c_void_p),
+                                   C.byref(n), stream_handle(stream)))
+    return out, ang
+
+
+def halfscan_feather(geometry, sino, stream=None):
+    """Projections::HalfScanFeather, in place on a device sinogram."""
+    check(lib().ctgpu_halfscan_feather(C.byref(geometry), _ptr(sino), sino.shape[0],
+                                       sino.shape[1], stream_handle(stream)))
+    return sino
+
+
+def _to_device(a):
+    torch = _torch()
+    a = np.ascontiguousarray(a, np.float32)
+    t = torch.zeros((a.shape[0], pitch_for(a.shape[1])), dtype=torch.float32, device="cuda")
+    t[:, :a.shape[1]] = torch.from_numpy(a).cuda()
+    return t
+
+
+def helical180li_host(geometry, data, interp_view=-1):
+    g = Geometry.from_buffer_copy(geometry)
+    g.n_view = data.shape[0]
+    out, ang = helical180li(g, _to_device(data), interp_view)
+    from . import sync
+    sync()
+    return out[:, :data.shape[1]].cpu().numpy(), ang
+
+
+def halfscan_feather_host(geometry, data):
+    g = Geometry.from_buffer_copy(geometry)
+    g.n_view = data.shape[0]
+    t = _to_device(data)
+    halfscan_feather(g, t)
+    from . import sync
+    sync()
+    return t[:, :data.shape[1]].cpu().numpy()

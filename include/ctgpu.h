@@ -1,0 +1,195 @@
+/* ctgpu.h -- C ABI of the GB300 simulate-and-reconstruct library (libctgpu.so).
+ *
+ * Drop-in boundary for CTSim's hot path: analytic phantom ray-sums
+ * (Scanner::collectProjections), projection filtering (ProcessSignal) and
+ * backprojection (Backprojector) as driven by Reconstructor, plus the helical
+ * 180LI / half-scan pre-step.  Every entry point below names the CTSim 5.2.0
+ * interface (file:line) whose behaviour it reproduces.  Plain C types only:
+ * pointers, sizes, doubles; no C++ or torch types cross this boundary.
+ *
+ * Conventions
+ *   - Return value: CTGPU_OK (0) or one of the CTGPU_ERR_* codes; the message
+ *     of the last failure on the calling thread is ctgpu_last_error().
+ *   - Names (geometry, filter, method, generation, interpolation,
+ *     backprojector) use the reference's case-insensitive name tables,
+ *     including its quirks ("shepp" selects the |w|*sinc response and
+ *     "abs_sinc" the Shepp response; the method "fouier-table" is spelt as in
+ *     the reference).
+ *   - d_ prefix: device pointer (cudaMalloc'ed or equivalent); h_ prefix: host
+ *     pointer.  Sinograms are row-major [view][detector] FP32 with a row pitch
+ *     in floats (>= n_det; a multiple of 4 keeps rows 16-byte aligned for the
+ *     bulk copies the backprojector issues).  Images are column-major
+ *     [ix][iy] FP32 like CTSim's ImageFile (v[ix][iy]).
+ *   - `stream` is a cudaStream_t passed as void* (NULL = default stream).
+ *     Calls taking a stream only enqueue work; ctgpu_sync() waits and reports
+ *     device-side failures (a bounded wait that gave up).
+ *   - Handles are not thread-safe; use one per thread, like the reference's
+ *     one-Reconstructor-per-thread model (src/threadrecon.cpp:219-255).
+ */
+#ifndef CTGPU_H
+#define CTGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CTGPU_ABI_VERSION 1
+
+enum {
+  CTGPU_OK = 0,
+  CTGPU_ERR_INVALID = 1,      /* bad argument / name; the reference's fail() + failMessage() */
+  CTGPU_ERR_UNSUPPORTED = 2,  /* valid request the library does not implement */
+  CTGPU_ERR_CUDA = 3,         /* CUDA runtime error */
+  CTGPU_ERR_NOMEM = 4,        /* allocation failure */
+  CTGPU_ERR_TIMEOUT = 5,      /* a kernel's bounded wait gave up (see ctgpu_sync) */
+  CTGPU_ERR_IO = 6            /* file could not be read */
+};
+
+/* geometry ids: libctsim/scanner.cpp:29-33 */
+enum { CTGPU_GEOMETRY_PARALLEL = 0, CTGPU_GEOMETRY_EQUIANGULAR = 1, CTGPU_GEOMETRY_EQUILINEAR = 2 };
+
+/* Message for the last non-OK return on this thread ("" if none). */
+const char* ctgpu_last_error(void);
+int ctgpu_abi_version(void);
+
+/* Waits for `stream` and reports CTGPU_ERR_TIMEOUT if a kernel's bounded
+ * shared-memory pipeline wait expired since the last call (the kernel then
+ * stopped early and its output is invalid), CTGPU_ERR_CUDA on a CUDA error. */
+int ctgpu_sync(void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Phantom -- replaces Phantom / PhantomElement (libctsim/phantom.cpp:58-256, */
+/* :554-756).  Elements keep the reference's list order (last added first)   */
+/* and the 360-point outline bounding box used to pre-reject rays.           */
+/* ------------------------------------------------------------------------ */
+typedef struct ctgpu_phantom ctgpu_phantom;
+
+/* Phantom::Phantom() -- empty phantom */
+int ctgpu_phantom_create(ctgpu_phantom** out);
+/* Phantom::createFromPhantom (phantom.cpp:128-170): "herman", "shepp-logan", "unit-pulse" */
+int ctgpu_phantom_create_builtin(const char* name, ctgpu_phantom** out);
+/* Phantom::addPElem (phantom.cpp:237-256); type: rectangle|triangle|ellipse|sector|segment */
+int ctgpu_phantom_add_element(ctgpu_phantom* p, const char* type, double cx, double cy, double u,
+                              double v, double rot_deg, double atten);
+/* Phantom::createFromFile (phantom.cpp:184-213): lines "type cx cy u v rot atten" */
+int ctgpu_phantom_read_file(ctgpu_phantom* p, const char* filename);
+/* xmin, xmax, ymin, ymax of the union of element bounding boxes (phantom.cpp:250-253) */
+int ctgpu_phantom_bounds(const ctgpu_phantom* p, double bounds[4], int* n_elements);
+void ctgpu_phantom_destroy(ctgpu_phantom* p);
+
+/* ------------------------------------------------------------------------ */
+/* Scan geometry: the fields of a .pj header (libctsim/projections.cpp:485-546) */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int32_t geometry;           /* CTGPU_GEOMETRY_* */
+  int32_t n_det;
+  int32_t n_view;
+  int32_t reserved;
+  double rot_start, rot_inc;
+  double det_start, det_inc;
+  double view_diameter, focal_length, source_detector_length, fan_beam_angle;
+} ctgpu_geometry;
+
+/* ------------------------------------------------------------------------ */
+/* Scanner -- replaces Scanner::Scanner (libctsim/scanner.cpp:86-224) and   */
+/* Scanner::collectProjections (:280-533)                                    */
+/* ------------------------------------------------------------------------ */
+typedef struct ctgpu_scanner ctgpu_scanner;
+
+/* Scanner::Scanner: rot_angle in radians (phm2pj passes fraction * 2*pi),
+ * ratios as in tools/phm2pj.cpp (defaults 2, 2, 1, 1). */
+int ctgpu_scanner_create(const ctgpu_phantom* p, const char* geometry_name, int n_det, int n_view,
+                         int offset_view, int n_sample, double rot_angle,
+                         double focal_length_ratio, double center_detector_ratio,
+                         double view_ratio, double scan_ratio, ctgpu_scanner** out);
+/* Projections::initFromScanner (projections.cpp:145-161) */
+int ctgpu_scanner_geometry(const ctgpu_scanner* s, ctgpu_geometry* out);
+/* Scanner::collectProjections(proj, phm, iStartView, iNumViews, iOffsetView,
+ * iStorageOffset) (scanner.cpp:295-419): ray-sums of views
+ * [start_view, start_view + n_views) into rows storage_offset.. of d_sino;
+ * the view angles (FP64, accumulated exactly as the reference) go to
+ * h_view_angles[storage_offset..] when non-NULL. */
+int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int start_view,
+                              int n_views, int offset_view, int storage_offset, float* d_sino,
+                              int sino_pitch, double* h_view_angles, void* stream);
+/* Same with a host sinogram [n_view][n_det]; copies in the call, synchronous. */
+int ctgpu_collect_projections_host(ctgpu_scanner* s, const ctgpu_phantom* p, int start_view,
+                                   int n_views, int offset_view, int storage_offset,
+                                   float* h_sino, double* h_view_angles);
+void ctgpu_scanner_destroy(ctgpu_scanner* s);
+
+/* ------------------------------------------------------------------------ */
+/* Reconstruction -- replaces Reconstructor (libctsim/reconstruct.cpp:50-239) */
+/* with its ProcessSignal (procsignal.cpp:82-629) and Backprojector          */
+/* (backprojectors.cpp:100-743)                                              */
+/* ------------------------------------------------------------------------ */
+typedef struct ctgpu_recon ctgpu_recon;
+typedef struct { double x_min, y_min, x_max, y_max; } ctgpu_roi;   /* ReconstructionROI */
+
+/* Reconstructor::Reconstructor: filter bandwidth 1/det_inc and domain "spatial"
+ * as the reference passes them.  interp_factor (preinterpolation) is accepted
+ * for the convolution and O(n^2) Fourier methods, where the reference ignores
+ * it, and rejected (CTGPU_ERR_UNSUPPORTED) for "fft", whose FFTW-only
+ * preinterpolated output has no reference to match. */
+int ctgpu_recon_create(const ctgpu_geometry* g, int nx, int ny, const char* filter_name,
+                       double filter_param, const char* filter_method, int zeropad,
+                       const char* filter_generation, const char* interp_name,
+                       int interp_factor, const char* backproj_name, const ctgpu_roi* roi,
+                       ctgpu_recon** out);
+/* image axis extent and increments (Backproject::Backproject, backprojectors.cpp:284-315) */
+int ctgpu_recon_image_axes(const ctgpu_recon* r, double extent[4], double increment[2]);
+/* ProcessSignal::filterSignal for n_views rows (procsignal.cpp:543-629) */
+int ctgpu_recon_filter(ctgpu_recon* r, const float* d_sino, int sino_pitch, int n_views,
+                       float* d_filtered, int filtered_pitch, void* stream);
+/* Backprojector::BackprojectView for n_views filtered rows with their view
+ * angles; accumulate=0 clears d_image first (Backproject ctor's
+ * arrayDataClear), 1 adds to it. */
+int ctgpu_recon_backproject(ctgpu_recon* r, const float* d_filtered, int filtered_pitch,
+                            const double* h_view_angles, int n_views, float* d_image,
+                            int accumulate, void* stream);
+/* Backprojector::PostProcessing (backprojectors.cpp:324-336, :435-442) */
+int ctgpu_recon_postprocess(ctgpu_recon* r, float* d_image, void* stream);
+/* Reconstructor::reconstructView(start, count) (+ postProcessing when
+ * CTGPU_RUN_POSTPROCESS is set, i.e. reconstructAllViews). d_sino holds all
+ * n_view rows; h_view_angles all n_view angles. */
+#define CTGPU_RUN_POSTPROCESS 1
+#define CTGPU_RUN_ACCUMULATE 2
+int ctgpu_recon_run(ctgpu_recon* r, const float* d_sino, int sino_pitch,
+                    const double* h_view_angles, int start_view, int n_views, float* d_image,
+                    int flags, void* stream);
+/* Reconstructor::reconstructAllViews with host buffers: h_sino [n_view][n_det],
+ * h_image [nx][ny]; copies inside the call; synchronous. */
+int ctgpu_recon_run_host(ctgpu_recon* r, const float* h_sino, const double* h_view_angles,
+                         float* h_image);
+/* Forward projection of a pixel image: the exact transpose of the parallel
+ * table backprojector with linear interpolation (backprojectors.cpp:444-481)
+ * without its rotScale, times `scale`:
+ *   d_sino[v][d] = scale * sum_pixels image * w(pixel, view v, detector d).
+ * Parallel geometry, plans made with backproj "table" and interp "linear". */
+int ctgpu_recon_project(ctgpu_recon* r, const float* d_image, const double* h_view_angles,
+                        int n_views, float* d_sino, int sino_pitch, float scale, void* stream);
+void ctgpu_recon_destroy(ctgpu_recon* r);
+
+/* ------------------------------------------------------------------------ */
+/* Helical -- replaces Projections::Helical180LI / Helical180LI_Equiangular */
+/* and HalfScanFeather (libctsim/projections.cpp:200-439)                     */
+/* ------------------------------------------------------------------------ */
+/* number of output views, or the reference's error status (1: not enough
+ * data, 2: geometry not supported) as CTGPU_ERR_INVALID with a message */
+int ctgpu_helical180li_size(const ctgpu_geometry* g, int n_view_in, int interp_view,
+                            int* n_view_out);
+/* d_in [n_view_in][pitch] -> d_out [n_view_out][pitch]; FP64 weights,
+ * reference's FP32 accumulation order; h_out_angles[n_view_out] */
+int ctgpu_helical180li(const ctgpu_geometry* g, const float* d_in, int n_view_in, int interp_view,
+                       float* d_out, int pitch, double* h_out_angles, int* n_view_out,
+                       void* stream);
+/* in place on d_data [n_view][pitch] */
+int ctgpu_halfscan_feather(const ctgpu_geometry* g, float* d_data, int n_view, int pitch,
+                           void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CTGPU_H */

@@ -1,0 +1,226 @@
+"""GPU parity: libctgpu.so (called through its C ABI) against the reference's own
+outputs (golden fixtures) and the FP64 oracle.  Tolerance: rel-L2 <= 1e-5 for
+FP32 results against FP64 (the path's precision target); bit-exact where the
+reference itself computes in FP32 with FP64 weights (helical)."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+SCANS = {  # name: (phantom, geometry, nray, Scanner kwargs) -- tests/golden/make_golden.py
+    "c1": ("shepp-logan", "parallel", 2, {}),
+    "herman_par": ("herman", "parallel", 2, {}),
+    "shepp_eqa": ("shepp-logan", "equiangular", 1, {}),
+    "shepp_eqa_even": ("shepp-logan", "equiangular", 3, {}),
+    "herman_eql": ("herman", "equilinear", 2, {}),
+    "herman_eqa": ("herman", "equiangular", 1, {}),
+    "shepp_par_even": ("shepp-logan", "parallel", 1, {"offsetView": 3}),
+    "pulse_par": ("unit-pulse", "parallel", 1, {}),
+    "shepp_eql_ratio": ("shepp-logan", "equilinear", 1,
+                        {"focalLengthRatio": 3.0, "centerDetectorRatio": 1.5, "viewRatio": 1.2,
+                         "scanRatio": 0.9}),
+}
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import ctsim_gb300 as cg
+    from ctsim_gb300 import device
+    return torch, cg, device
+
+
+def geom_from_hdr(cg, hdr):
+    g, nd, nv, rs, ri, ds, di, vd, fl, sdl, fan = hdr
+    return cg.Geometry(int(g), int(nd), int(nv), 0, rs, ri, ds, di, vd, fl, sdl, fan)
+
+
+def to_dev(torch, device, a):
+    t = device.alloc_sinogram(a.shape[0], a.shape[1])
+    t[:, :a.shape[1]] = torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+    return t
+
+
+@pytest.mark.parametrize("name", list(SCANS))
+def test_raysums_match_reference(gpu, golden, name):
+    torch, cg, device = gpu
+    d = golden("scans")
+    phm, geo, nray, kw = SCANS[name]
+    hdr = d[name + "/hdr"]
+    ph = cg.Phantom(phm)
+    sc = cg.Scanner(ph, geo, int(hdr[1]), int(hdr[2]), nSample=nray, **kw)
+    g = sc.geometry()
+    assert g.det_inc == hdr[6] and g.view_diameter == hdr[7] and g.fan_beam_angle == hdr[10]
+    sino = device.alloc_sinogram(g.n_view, g.n_det)
+    ang = device.raysums(sc, ph, sino)
+    cg.sync()
+    np.testing.assert_array_equal(ang, d[name + "/angles"])
+    out = sino[:, :g.n_det].cpu().numpy()
+    ref = d[name + "/data"]
+    assert rel_l2(out, ref) < TOL, rel_l2(out, ref)
+    assert np.abs(out - ref).max() <= 1e-4 * max(np.abs(ref).max(), 1e-30)
+
+
+def test_raysums_subrange_and_storage_offset(gpu, golden):
+    torch, cg, device = gpu
+    d = golden("scans")
+    ph = cg.Phantom("herman")
+    sc = cg.Scanner(ph, "parallel", 101, 60, nSample=2)
+    sino = device.alloc_sinogram(60, 101)
+    a1 = device.raysums(sc, ph, sino, start_view=0, n_views=25)
+    a2 = device.raysums(sc, ph, sino, start_view=25, n_views=35)
+    cg.sync()
+    out = sino[:, :101].cpu().numpy()
+    assert rel_l2(out, d["herman_par/data"]) < TOL
+    np.testing.assert_array_equal(np.concatenate([a1[:25], a2[25:]]), d["herman_par/angles"])
+
+
+def test_raysums_host_entry_point(gpu, golden):
+    torch, cg, device = gpu
+    d = golden("scans")
+    ph = cg.Phantom("shepp-logan")
+    sc = cg.Scanner(ph, "equiangular", 133, 96)
+    pj = cg.Projections.from_scanner(sc)
+    sc.collectProjections(pj, ph)
+    assert rel_l2(pj.data, d["shepp_eqa/data"]) < TOL
+    np.testing.assert_array_equal(pj.angles, d["shepp_eqa/angles"])
+
+
+def test_reconstructions_match_reference(gpu, golden):
+    torch, cg, device = gpu
+    scans = golden("scans")
+    rec = golden("recons")
+    n = len([k for k in rec.files if k.endswith("/cfg")])
+    worst = 0
+    for k in range(n):
+        sc, nx, ny, bp, ip, flt, meth, zp, gen, prm = rec["%d/cfg" % k]
+        g = geom_from_hdr(cg, scans[sc + "/hdr"])
+        sino = to_dev(torch, device, scans[sc + "/data"])
+        plan = device.ReconPlan(g, int(nx), int(ny), flt, float(prm), meth, int(zp), gen, ip, 1, bp)
+        img = torch.zeros((int(nx), int(ny)), dtype=torch.float32, device="cuda")
+        plan.run(sino, scans[sc + "/angles"], img)
+        cg.sync()
+        ref = rec["%d/image64" % k]
+        e = rel_l2(img.cpu().numpy(), ref)
+        worst = max(worst, e)
+        assert e < TOL, "case %d %s: rel-L2 %.3g" % (k, rec["%d/cfg" % k], e)
+    print("worst reconstruction rel-L2 %.3g" % worst)
+
+
+def test_reconstructor_host_api(gpu, golden):
+    torch, cg, device = gpu
+    scans = golden("scans")
+    rec = golden("recons")
+    pj = cg.Projections(320, 367, 0, 0, 0, *scans["c1/hdr"][4:],
+                        angles=scans["c1/angles"], data=scans["c1/data"])
+    im = cg.ImageFile(256, 256)
+    r = cg.Reconstructor(pj, im, "abs_bandlimit", -1, "convolution", 1, "direct", "linear", 1,
+                         "table")
+    r.reconstructAllViews()
+    assert rel_l2(im.data, rec["0/image64"]) < TOL
+
+
+def test_filter_matches_oracle(gpu, oracle):
+    torch, cg, device = gpu
+    rng = np.random.default_rng(3)
+    nd, nv = 733, 5
+    x = rng.random((nv, nd)).astype(np.float32)
+    xd = to_dev(torch, device, x)
+    cases = [("abs_bandlimit", "convolution", 1, "direct", 0),
+             ("abs_hamming", "fft", 2, "direct", 1),
+             ("abs_hamming", "fourier", 1, "direct", 2),
+             ("shepp", "fft", 2, "direct", 0),
+             ("abs_cosine", "convolution", 1, "inverse-fourier", 0),
+             ("abs_hanning", "fft", 1, "inverse-fourier", 1),
+             ("abs_sinc", "convolution", 1, "direct", 2),
+             ("triangle", "fourier", 0, "direct", 0)]
+    names = ("parallel", "equiangular", "equilinear")
+    for flt, meth, zp, gen, geo in cases:
+        g = cg.Geometry(geo, nd, nv, 0, 0, 0.01, 0, 0.0021, 2.6, 2.6, 5.2, 1.0)
+        plan = device.ReconPlan(g, 16, 16, flt, 0.54, meth, zp, gen, "linear", 1, "table")
+        out = device.alloc_sinogram(nv, nd)
+        plan.filter(xd, out)
+        cg.sync()
+        ref = oracle.ProcessSignal(flt, meth, nd, 0.0021, param=0.54,
+                                   generation=gen, zeropad=zp, geometry=names[geo],
+                                   focal_length=2.6, sdl=5.2).filter(x)
+        e = rel_l2(out[:, :nd].cpu().numpy(), ref)
+        assert e < TOL, (flt, meth, zp, gen, geo, e)
+
+
+def test_helical_bit_exact(gpu, golden):
+    torch, cg, device = gpu
+    d = golden("helical")
+    for k in range(2):
+        g = geom_from_hdr(cg, d["%d/in_hdr" % k])
+        sino = to_dev(torch, device, d["%d/in_data" % k])
+        out, ang = device.helical180li(g, sino, int(d["%d/interpview" % k]))
+        g.n_view = out.shape[0]
+        device.halfscan_feather(g, out)
+        cg.sync()
+        np.testing.assert_array_equal(ang, d["%d/out_angles" % k])
+        np.testing.assert_array_equal(out[:, :g.n_det].cpu().numpy(), d["%d/out_data" % k])
+
+
+def test_projector_is_adjoint_of_backprojector(gpu):
+    torch, cg, device = gpu
+    g = cg.Geometry(0, 129, 90, 0, 0, np.pi / 90, 0, 0.021, 2.6, 2.6, 5.2, 0.0)
+    ang = np.arange(90) * (np.pi / 90)
+    plan = device.ReconPlan(g, 96, 80, "abs_bandlimit", -1, "convolution", 1, "direct", "linear",
+                            1, "table")
+    torch.manual_seed(0)
+    x = torch.randn((96, 80), device="cuda")
+    y = device.alloc_sinogram(90, 129)
+    y[:, :129] = torch.randn((90, 129), device="cuda")
+    ax = device.alloc_sinogram(90, 129)
+    plan.project(x, ang, ax)
+    bty = torch.zeros((96, 80), device="cuda")
+    plan.backproject(y, ang, bty)
+    cg.sync()
+    lhs = float((ax[:, :129].double() * y[:, :129].double()).sum())
+    rhs = float((x.double() * bty.double()).sum())
+    assert abs(lhs - rhs) <= 1e-6 * abs(lhs), (lhs, rhs)
+
+
+def test_projector_matches_oracle(gpu, oracle):
+    torch, cg, device = gpu
+    g = cg.Geometry(0, 129, 45, 0, 0, np.pi / 45, 0, 0.021, 2.6, 2.6, 5.2, 0.0)
+    og = oracle.Geom(0, 129, 45, np.pi / 45, 0.021, 2.6, 5.2, 2.6, 0.0)
+    ang = np.arange(45) * (np.pi / 45)
+    plan = device.ReconPlan(g, 64, 64, "abs_bandlimit", -1, "convolution", 1, "direct", "linear",
+                            1, "table")
+    rng = np.random.default_rng(2)
+    x = rng.random((64, 64))
+    ax = device.alloc_sinogram(45, 129)
+    plan.project(torch.from_numpy(x.astype(np.float32)).cuda(), ang, ax)
+    cg.sync()
+    ref = oracle.project_image(og, x, ang)
+    assert rel_l2(ax[:, :129].cpu().numpy(), ref) < TOL
+
+
+def test_zero_views_and_accumulate(gpu, golden):
+    torch, cg, device = gpu
+    scans = golden("scans")
+    g = geom_from_hdr(cg, scans["herman_par/hdr"])
+    sino = to_dev(torch, device, scans["herman_par/data"])
+    ang = scans["herman_par/angles"]
+    plan = device.ReconPlan(g, 40, 40, "abs_bandlimit", -1, "convolution", 1, "direct", "cubic", 1,
+                            "idiff")
+    full = torch.zeros((40, 40), device="cuda")
+    plan.run(sino, ang, full)
+    # view sub-ranges accumulated, then PostProcessing: reconstructView(start, count) x 2
+    part = torch.full((40, 40), 7.0, device="cuda")
+    plan.run(sino, ang, part, start_view=0, n_views=23, postprocess=False)   # overwrites
+    plan.run(sino, ang, part, start_view=23, n_views=37, postprocess=False, accumulate=True)
+    plan.postprocess(part)
+    cg.sync()
+    assert rel_l2(part.cpu().numpy(), full.cpu().numpy()) < 1e-6
+    plan.run(sino, ang, part, start_view=0, n_views=23, postprocess=False)
+    plan.run(sino, ang, part, start_view=23, n_views=37, postprocess=True, accumulate=True)
+    cg.sync()
+    assert rel_l2(part.cpu().numpy(), full.cpu().numpy()) < 1e-6
