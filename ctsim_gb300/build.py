@@ -21,12 +21,19 @@ LIB = os.path.join(PKG, "libctgpu.so")
 TOOL = os.path.join(PKG, "ctgpu_ctsimtext")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-Wall",
+# Host code keeps the reference's FP64 rounding: no contraction into FMAs
+# (aarch64 compilers contract by default), so geometry, filters and view
+# steps come out bit-identical on x86 and Arm.
+NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17",
+                  "-Xcompiler", "-fPIC,-O2,-Wall,-ffp-contract=off",
                   "-I" + os.path.join(ROOT, "include")]
+# per-file device flags: the helical weights are FP64 expressions the
+# reference evaluates without fused multiply-adds
+FILE_FLAGS = {"k_helical.cu": ["--fmad=false"]}
 
 LIB_SOURCES = ["k_common.cu", "k_raysum.cu", "k_filter.cu", "k_backproject.cu", "k_helical.cu",
-               "ctgpu_api.cpp", "filter_design.cpp"]
-TOOL_SOURCES = []
+               "ctgpu_api.cpp", "filter_design.cpp", "ctsim_api.cpp"]
+TOOL_SOURCES = ["tools/ctsimtext.cpp"]
 
 
 def nvcc():
@@ -53,7 +60,7 @@ def _compile(src, force):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if not force and not _stale(obj, [src] + _headers()):
         return obj, None
-    cmd = [nvcc()] + NVFLAGS + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + NVFLAGS + FILE_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         return obj, "%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr)

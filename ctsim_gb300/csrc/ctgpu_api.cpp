@@ -708,6 +708,11 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
   L.focalLength = r->g.focal_length;
   L.sdl = r->g.source_detector_length;
   L.rotScale = r->rotScale;
+  {
+    double xm = std::fmax(std::fabs(r->xMin), std::fabs(r->xMax));
+    double ym = std::fmax(std::fabs(r->yMin), std::fabs(r->yMax));
+    L.minSourceDist = r->g.focal_length - std::sqrt(xm * xm + ym * ym);
+  }
   L.angles = r->d_angles;
   L.filtered = d_filtered;
   L.image = d_image;

@@ -56,6 +56,7 @@ struct BackprojLaunch {
   int nDet, nx, ny, nViews, pitch;
   int iDetCenter;
   double detInc, xMin, yMin, xInc, yInc, focalLength, sdl, rotScale;
+  double minSourceDist;   // fan beams: lower bound of the source-to-pixel distance
   const double* angles;   // device, nViews
   const float* filtered;  // device, [nViews][pitch]
   float* image;           // device, [nx][ny]
