@@ -1,0 +1,345 @@
+"""Benchmark: FBP pixel-view updates/s (and ray-sums/s) on GB300 vs the CPU path.
+
+Workload (one GPU): the equiangular fan-beam configuration -- seeded
+12-ellipse phantoms, 733 detectors x 720 views over 360 degrees, focal length
+2 view radii, abs_hamming(0.54) filter by FFT with zeropad 2, cubic
+interpolation, 512 x 512 FP32 image.  A step reconstructs a batch of B such
+slices (default 64) whose sinograms were simulated on the device beforehand;
+the batch's sinograms (B x 2.1 MB) and images (B x 1 MB) exceed the 129 MB L2,
+so no flush is needed between steps.  The ray-sum phase (simulating the same
+batch) is timed separately over the same number of steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl reference]
+
+--impl reference times the CPU implementation of the same path on the host's
+cores: the FP64 restatement in oracle/ (the reference's own binaries are not
+available on this machine), FFT filtering, table backprojection with cubic
+interpolation, views split over all threads.  One JSON line on rank 0.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DET, N_VIEW, NX = 733, 720, 512
+PV_PER_SLICE = NX * NX * N_VIEW
+RAYS_PER_SLICE = N_DET * N_VIEW
+METRIC = "FBP pixel-view updates/s"
+UNIT = "pixel-view updates/s"
+# algorithmic work per unit for the dominant kernel (equiangular, cubic):
+# 4 samples x 4 B gathered per pixel-view update; 30 + 30 FLOP
+BYTES_PER_PV = 16
+FLOP_PER_PV = 60
+CONFIG_NAME = ("equiangular 733 det x 720 views (360 deg), 12 random ellipses, abs_hamming 0.54 "
+               "FFT zeropad 2, cubic, 512x512 FP32")
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+def reduce_max(value, world):
+    """max over ranks (the timing rule); identity on one rank"""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def cpu_fbp_rate(seed, seconds=10.0, nthreads=None, views=None):
+    """The CPU path (FP64 oracle port) on a bounded sample: FBP of whole slices
+    until `seconds` have passed (at least one).  Returns (pv/s, sample text, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "oracle"], check=True)
+    import pyoracle as po
+    from ctsim_gb300 import phantoms
+    nthreads = nthreads or (os.cpu_count() or 1)
+    ph = po.Phantom(elements=phantoms.random_ellipses(seed, 12))
+    sc = po.Scanner(ph, "equiangular", N_DET, N_VIEW, nsample=1)
+    sino, ang = sc.collect(nthreads=nthreads)
+    nv = N_VIEW if views is None else views
+    done, t0 = 0, time.perf_counter()
+    while True:
+        po.reconstruct(sc.geom(), sino[:nv].astype(np.float32), ang[:nv], NX, NX,
+                       filter_name="abs_hamming", param=0.54, method="fft", zeropad=2,
+                       backproj="table", interp="cubic", nthreads=nthreads)
+        done += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    pv = done * NX * NX * nv
+    return pv / el, "%d slice(s) of %d views, FFT zeropad 2, table/cubic, %d threads, %.1f s" % (
+        done, nv, nthreads, el), nthreads
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    rates = []
+    sample = None
+    for i in range(args.warmup + args.steps):
+        r, sample, threads = cpu_fbp_rate(seed=1000 + i, seconds=0.0, views=args.ref_views)
+        if i >= args.warmup:
+            rates.append(r)
+    value = float(np.mean(rates))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": PV_PER_SLICE * (args.ref_views or N_VIEW) / N_VIEW / value * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded random-ellipse phantoms)",
+            "config": {"workload": CONFIG_NAME, "step": "one slice per step",
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def traffic_per_launch():
+    """DRAM bytes per backprojection launch from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "backproject_equiangular_cubic_512_ncu.md")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    return None
+
+
+def run_gpu(args):
+    import torch
+    import ctsim_gb300 as cg
+    from ctsim_gb300 import device, phantoms
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    B = args.batch
+    stream = torch.cuda.current_stream()
+    # --- inputs: B seeded phantoms, simulated on the device --------------------
+    phs, scs = [], []
+    for b in range(B):
+        ph = phantoms.make_phantom(phantoms.random_ellipses(seed=rank * 100000 + b, n=12))
+        phs.append(ph)
+        scs.append(cg.Scanner(ph, "equiangular", N_DET, N_VIEW, nSample=1))
+    g = scs[0].geometry()
+    sinos = [device.alloc_sinogram(N_VIEW, N_DET) for _ in range(B)]
+    images = [torch.zeros((NX, NX), device="cuda") for _ in range(B)]
+    plan = device.ReconPlan(g, NX, NX, "abs_hamming", 0.54, "fft", 2, "direct", "cubic", 1, "table")
+    angles = [None] * B
+
+    def raysum_step():
+        for b in range(B):
+            angles[b] = device.raysums(scs[b], phs[b], sinos[b])
+
+    def fbp_step(bp_events=None):
+        for b in range(B):
+            plan.filter(sinos[b], plan_filtered)
+            if bp_events is not None:
+                bp_events[b][0].record(stream)
+            plan.backproject(plan_filtered, angles[b], images[b])
+            if bp_events is not None:
+                bp_events[b][1].record(stream)
+            plan.postprocess(images[b])
+
+    plan_filtered = device.alloc_sinogram(N_VIEW, N_DET)
+    for _ in range(max(args.warmup, 1)):
+        raysum_step()
+        fbp_step()
+    cg.sync()
+
+    # --- timed: FBP --------------------------------------------------------------
+    bp_ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(B)] for _ in range(args.steps)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for k in range(args.steps):
+            fbp_step(bp_ev[k])
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    cg.sync()
+    fbp_ms = reduce_max(e0.elapsed_time(e1), world)
+    bp_ms = [s.elapsed_time(e) for step in bp_ev for (s, e) in step]
+    bp_avg_ms = float(np.mean(bp_ms))
+
+    # --- timed: ray-sums -----------------------------------------------------------
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    r0.record(stream)
+    for k in range(args.steps):
+        raysum_step()
+    r1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    cg.sync()
+    ray_ms = reduce_max(r0.elapsed_time(r1), world)
+
+    # --- e2e: the C-ABI host-buffer reconstruct call, copies inside ----------------
+    host_sinos = [s[:, :N_DET].cpu().numpy() for s in sinos]
+    for b in range(min(B, 2)):
+        plan.run_host(host_sinos[b], angles[b])
+    barrier(world)
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 5))
+    for k in range(e2e_steps):
+        for b in range(B):
+            out = plan.run_host(host_sinos[b], angles[b])
+    e2e_s = reduce_max(time.perf_counter() - t0, world)
+    # parity spot check of the last slice against the device path
+    dev_img = images[B - 1].cpu().numpy()
+    e2e_err = float(np.linalg.norm(out - dev_img) / np.linalg.norm(dev_img))
+
+    if rank != 0:
+        return 0
+    steps = args.steps
+    total_pv = PV_PER_SLICE * B * steps * world
+    value = total_pv / (fbp_ms / 1e3)
+    hbm, src = peaks()
+    achieved = BYTES_PER_PV * PV_PER_SLICE / (bp_avg_ms / 1e-3) / 1e9
+    cpu_v, cpu_sample, cpu_threads = cpu_fbp_rate(seed=7, seconds=args.cpu_seconds,
+                                                  views=args.ref_views)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": fbp_ms / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded random-ellipse phantoms, simulated on the device)",
+        "config": {"workload": CONFIG_NAME, "batch_slices_per_step": B,
+                   "l2": "inputs larger than L2 (%d sinograms x 2.1 MB + %d images x 1 MB)" % (B, B),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "raysums": {"metric": "ray-sums/s", "value": RAYS_PER_SLICE * B * steps * world / (ray_ms / 1e3),
+                    "ms_per_step": ray_ms / steps,
+                    "ray_element_pairs_per_s": RAYS_PER_SLICE * 12 * B * steps * world / (ray_ms / 1e3)},
+        "roofline": {"kernel": "backproject_table_kernel<equiangular,cubic>", "bound": "hbm",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": src, "traffic": traffic_per_launch(),
+                     "algorithmic_bytes_per_launch": BYTES_PER_PV * PV_PER_SLICE,
+                     "avg_launch_ms": bp_avg_ms,
+                     "fp32_tflops": FLOP_PER_PV * PV_PER_SLICE / (bp_avg_ms / 1e3) / 1e12},
+        "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
+                         "sample": cpu_sample},
+        "e2e": {"value": PV_PER_SLICE * B * e2e_steps * world / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": B * (N_VIEW * N_DET * 4 + N_VIEW * 8),
+                "d2h_bytes_per_step": B * NX * NX * 4,
+                "steps": e2e_steps, "path": "ctgpu_recon_run_host (pageable host buffers)",
+                "parity_vs_device_rel_l2": e2e_err},
+        "gpu_launches": steps * B * 3,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-views", type=int, default=None,
+                    help="views per CPU sample slice (default: all 720)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -39,7 +39,14 @@ struct ElemView {
   float cpsi, spsi;  // equiangular: cos/sin of psi'
   float ra, rb;      // parallel: ray direction in the element frame
   int live;          // 0: no ray of this view can meet the element
+  int pad;
 };
+static_assert(sizeof(ElemView) % 16 == 0, "ElemView records keep 16-byte alignment");
+
+// byte offset of the per-sub-sample direction table after the element records
+__host__ __device__ inline size_t dir_table_offset(int nRecords) {
+  return ((size_t)nRecords * sizeof(ElemView) + 15) & ~(size_t)15;
+}
 
 __device__ __forceinline__ double cross2(double ax, double ay, double bx, double by) {
   return ax * by - ay * bx;
@@ -290,7 +297,7 @@ __device__ void setup_element(const RaysumLaunch& L, const ViewGeom& g, const PE
 
 template <int GEOM>
 __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
-  extern __shared__ ElemView ev[];
+  extern __shared__ __align__(16) ElemView ev[];
   const int view = blockIdx.x;
   const ViewPos vp = L.views[view];
   ViewGeom g;
@@ -298,7 +305,8 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
   const int nS = L.nSample;
   const int nSub = (GEOM == kParallel) ? nS : 1;
   const int nElem = L.nElem;
-  float2* sdir = reinterpret_cast<float2*>(ev + nElem * nSub);   // parallel: per sub-sample
+  float2* sdir = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(ev) +
+                                           dir_table_offset(nElem * nSub));   // per sub-sample
   for (int k = threadIdx.x; k < nElem * nSub; k += blockDim.x)
     setup_element<GEOM>(L, g, L.elems[k / nSub], k % nSub, ev[k]);
   if (GEOM == kParallel) {
@@ -406,7 +414,7 @@ __global__ void unit_pulse_kernel(float* sino, int nViews, int nDet, int pitch, 
 cudaError_t launch_raysum(const RaysumLaunch& L, cudaStream_t s) {
   if (L.nViews <= 0) return cudaSuccess;
   int nSub = (L.geometry == kParallel) ? L.nSample : 1;
-  size_t smem = sizeof(ElemView) * (size_t)(L.nElem > 0 ? L.nElem : 1) * nSub +
+  size_t smem = dir_table_offset((L.nElem > 0 ? L.nElem : 1) * nSub) +
                 sizeof(float2) * (size_t)L.nSample;
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   dim3 grid(L.nViews), block(128);
