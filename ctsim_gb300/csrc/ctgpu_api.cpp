@@ -656,9 +656,21 @@ int ctgpu_recon_filter(ctgpu_recon* r, const float* d_sino, int sinoPitch, int n
 // Backprojection of nViews filtered rows; outScale multiplies this launch's sum.
 static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int pitch,
                                     const double* h_angles, int nViews, float* d_image,
-                                    int accumulate, float outScale, cudaStream_t st) {
+                                    int accumulate, float outScale, cudaStream_t st,
+                                    int nBatch = 1, size_t filtStride = 0,
+                                    size_t imageStride = 0) {
   if (nViews <= 0) {
-    if (!accumulate) CUDA_TRY(cudaMemsetAsync(d_image, 0, sizeof(float) * r->nx * r->ny, st));
+    if (!accumulate)
+      for (int b = 0; b < nBatch; b++)
+        CUDA_TRY(cudaMemsetAsync(d_image + b * imageStride, 0, sizeof(float) * r->nx * r->ny, st));
+    return ok();
+  }
+  if (nBatch > 1 && r->bproj == kDiff) {
+    for (int b = 0; b < nBatch; b++) {
+      int rc = recon_backproject_scaled(r, d_filtered + b * filtStride, pitch, h_angles, nViews,
+                                        d_image + b * imageStride, accumulate, outScale, st);
+      if (rc) return rc;
+    }
     return ok();
   }
   CUDA_TRY(ensure_device(r->d_angles, r->d_angles_cap, (size_t)nViews));
@@ -716,6 +728,9 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
   L.angles = r->d_angles;
   L.filtered = d_filtered;
   L.image = d_image;
+  L.nBatch = nBatch;
+  L.filtSliceStride = filtStride;
+  L.imageSliceStride = imageStride;
   L.accumulate = accumulate;
   L.outScale = outScale;
   L.status = status_pointer();
@@ -786,6 +801,57 @@ int ctgpu_recon_run_host(ctgpu_recon* r, const float* h_sino, const double* h_an
   return ctgpu_sync(nullptr);
 }
 
+int ctgpu_recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int sinoPitch,
+                          long long sinoSliceStride, const double* h_angles, float* d_images,
+                          long long imageSliceStride, int flags, void* stream) {
+  if (!r || !d_sinos || !h_angles || !d_images) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (nBatch < 1) return fail(CTGPU_ERR_INVALID, "batch size must be >= 1");
+  const int nView = r->g.n_view;
+  if (sinoPitch < r->g.n_det || sinoSliceStride < (long long)sinoPitch * nView ||
+      imageSliceStride < (long long)r->nx * r->ny)
+    return fail(CTGPU_ERR_INVALID, "pitch / slice strides too small");
+  if (flags & CTGPU_RUN_ACCUMULATE) return fail(CTGPU_ERR_UNSUPPORTED, "batched runs overwrite their images");
+  cudaStream_t st = (cudaStream_t)stream;
+  size_t fStride = (size_t)nView * r->pitch;
+  CUDA_TRY(ensure_device(r->d_filtered, r->d_filtered_cap, fStride * nBatch));
+  FilterLaunch F{};
+  F.nDet = r->g.n_det;
+  F.nViews = nView;
+  F.inPitch = sinoPitch;
+  F.outPitch = r->pitch;
+  F.taps = r->d_taps;
+  F.weights = r->d_weights;
+  for (int b = 0; b < nBatch; b++) {
+    F.in = d_sinos + (size_t)b * sinoSliceStride;
+    F.out = r->d_filtered + fStride * b;
+    CUDA_TRY(launch_filter(F, st));
+  }
+  float scale = raw_scale(r);
+  bool post = (flags & CTGPU_RUN_POSTPROCESS) != 0;
+  if (post && r->bproj != kTrig) scale = (float)(scale * r->rotScale);
+  return recon_backproject_scaled(r, r->d_filtered, r->pitch, h_angles, nView, d_images, 0, scale,
+                                  st, nBatch, fStride, (size_t)imageSliceStride);
+}
+
+int ctgpu_recon_backproject_batch(ctgpu_recon* r, int nBatch, const float* d_filtered, int pitch,
+                                  long long filtSliceStride, const double* h_angles, int nViews,
+                                  float* d_images, long long imageSliceStride, int flags,
+                                  void* stream) {
+  if (!r || !d_filtered || !h_angles || !d_images) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (nBatch < 1) return fail(CTGPU_ERR_INVALID, "batch size must be >= 1");
+  if (pitch < r->g.n_det || (pitch & 3) || (filtSliceStride & 3) ||
+      ((uintptr_t)d_filtered & 15) != 0)
+    return fail(CTGPU_ERR_INVALID, "filtered rows must be 16-byte aligned (pitch and slice stride multiples of 4)");
+  if (filtSliceStride < (long long)pitch * nViews || imageSliceStride < (long long)r->nx * r->ny)
+    return fail(CTGPU_ERR_INVALID, "slice strides too small");
+  if (flags & CTGPU_RUN_ACCUMULATE) return fail(CTGPU_ERR_UNSUPPORTED, "batched launches overwrite their images");
+  float scale = raw_scale(r);
+  if ((flags & CTGPU_RUN_POSTPROCESS) && r->bproj != kTrig) scale = (float)(scale * r->rotScale);
+  return recon_backproject_scaled(r, d_filtered, pitch, h_angles, nViews, d_images, 0, scale,
+                                  (cudaStream_t)stream, nBatch, (size_t)filtSliceStride,
+                                  (size_t)imageSliceStride);
+}
+
 int ctgpu_recon_project(ctgpu_recon* r, const float* d_image, const double* h_angles, int nViews,
                         float* d_sino, int pitch, float scale, void* stream) {
   if (!r || !d_image || !h_angles || !d_sino) return fail(CTGPU_ERR_INVALID, "null argument");
@@ -812,6 +878,7 @@ int ctgpu_recon_project(ctgpu_recon* r, const float* d_image, const double* h_an
   L.xInc = r->xInc;
   L.yInc = r->yInc;
   L.angles = r->d_angles;
+  L.nBatch = 1;
   L.status = status_pointer();
   CUDA_TRY(launch_project_table(L, d_image, d_sino, scale, st));
   return ok();

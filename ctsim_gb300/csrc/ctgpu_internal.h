@@ -58,8 +58,10 @@ struct BackprojLaunch {
   double detInc, xMin, yMin, xInc, yInc, focalLength, sdl, rotScale;
   double minSourceDist;   // fan beams: lower bound of the source-to-pixel distance
   const double* angles;   // device, nViews
-  const float* filtered;  // device, [nViews][pitch]
-  float* image;           // device, [nx][ny]
+  const float* filtered;  // device, [nBatch][nViews][pitch]
+  float* image;           // device, [nBatch][nx][ny]
+  int nBatch;             // slices sharing geometry and view angles (grid.z)
+  size_t filtSliceStride, imageSliceStride;   // elements between slices
   int accumulate;         // add into image instead of overwriting
   float outScale;         // applied to this launch's contribution (rotScale for trig)
   unsigned int* status;

@@ -99,6 +99,28 @@ class ReconPlan:
                                     _ptr(image), flags, stream_handle(stream)))
         return image
 
+    def run_batch(self, sinos, angles, images, postprocess=True, stream=None):
+        """sinos [B, n_view, pitch], images [B, nx, ny]: one filter launch per slice,
+        one backprojection launch for the batch."""
+        if not (sinos.is_contiguous() and images.is_contiguous()):
+            raise ValueError("batched tensors must be contiguous")
+        ang = np.ascontiguousarray(angles, np.float64)
+        check(lib().ctgpu_recon_run_batch(
+            self._h, sinos.shape[0], C.c_void_p(sinos.data_ptr()), sinos.shape[2],
+            sinos.stride(0), ang.ctypes.data_as(C.c_void_p), C.c_void_p(images.data_ptr()),
+            images.stride(0), RUN_POSTPROCESS if postprocess else 0, stream_handle(stream)))
+        return images
+
+    def backproject_batch(self, filtered, angles, images, postprocess=True, stream=None):
+        """filtered [B, n_view, pitch] -> images [B, nx, ny] in one launch."""
+        ang = np.ascontiguousarray(angles, np.float64)
+        check(lib().ctgpu_recon_backproject_batch(
+            self._h, filtered.shape[0], C.c_void_p(filtered.data_ptr()), filtered.shape[2],
+            filtered.stride(0), ang.ctypes.data_as(C.c_void_p), len(ang),
+            C.c_void_p(images.data_ptr()), images.stride(0),
+            RUN_POSTPROCESS if postprocess else 0, stream_handle(stream)))
+        return images
+
     def run_host(self, sino, angles):
         """reconstructAllViews with host numpy buffers (copies inside the call)."""
         s = np.ascontiguousarray(sino, np.float32)

@@ -163,6 +163,21 @@ int ctgpu_recon_run(ctgpu_recon* r, const float* d_sino, int sino_pitch,
  * h_image [nx][ny]; copies inside the call; synchronous. */
 int ctgpu_recon_run_host(ctgpu_recon* r, const float* h_sino, const double* h_view_angles,
                          float* h_image);
+/* Many slices of the same geometry and view angles in one launch per stage
+ * (the batched form of reconstructAllViews): d_sinos holds n_batch sinograms
+ * [n_view][sino_pitch] sino_slice_stride floats apart, d_images n_batch
+ * images [nx][ny] image_slice_stride floats apart; flags as ctgpu_recon_run
+ * (CTGPU_RUN_ACCUMULATE not supported). */
+int ctgpu_recon_run_batch(ctgpu_recon* r, int n_batch, const float* d_sinos, int sino_pitch,
+                          long long sino_slice_stride, const double* h_view_angles,
+                          float* d_images, long long image_slice_stride, int flags,
+                          void* stream);
+/* Backprojection of n_batch filtered sinograms (same geometry and angles) in
+ * one launch; flags: CTGPU_RUN_POSTPROCESS folds PostProcessing in. */
+int ctgpu_recon_backproject_batch(ctgpu_recon* r, int n_batch, const float* d_filtered,
+                                  int filtered_pitch, long long filtered_slice_stride,
+                                  const double* h_view_angles, int n_views, float* d_images,
+                                  long long image_slice_stride, int flags, void* stream);
 /* Forward projection of a pixel image: the exact transpose of the parallel
  * table backprojector with linear interpolation (backprojectors.cpp:444-481)
  * without its rotScale, times `scale`:

@@ -40,7 +40,9 @@ def test_projector_dot_product(setup):
     (gx,) = torch.autograd.grad((px * y).sum(), x)
     lhs = float((px.double() * y.double()).sum())
     rhs = float((x.detach().double() * gx.double()).sum())
-    assert abs(lhs - rhs) <= 1e-6 * abs(lhs), (lhs, rhs)
+    # <Ax, y> = <x, A^T y>, relative to the Cauchy-Schwarz scale |Ax| |y|
+    scale = float(px.double().norm() * y.double().norm())
+    assert abs(lhs - rhs) <= 1e-6 * scale, (lhs, rhs, scale)
 
 
 def test_fbp_dot_product(setup):
@@ -54,7 +56,8 @@ def test_fbp_dot_product(setup):
     (gs,) = torch.autograd.grad((f * w).sum(), s)
     lhs = float((f.double() * w.double()).sum())
     rhs = float((s.detach().double() * gs.double()).sum())
-    assert abs(lhs - rhs) <= 1e-6 * abs(lhs), (lhs, rhs)
+    scale = float(f.double().norm() * w.double().norm())
+    assert abs(lhs - rhs) <= 1e-6 * scale, (lhs, rhs, scale)
 
 
 def test_projection_loss_gradient(setup, oracle):
