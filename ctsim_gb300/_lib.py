@@ -74,6 +74,8 @@ SIGNATURES = {
     "ctgpu_helical180li_size": ([C.POINTER(Geometry), _i, _i, C.POINTER(_i)], _i),
     "ctgpu_helical180li": ([C.POINTER(Geometry), _p, _i, _i, _p, _i, _p, C.POINTER(_i), _p], _i),
     "ctgpu_halfscan_feather": ([C.POINTER(Geometry), _p, _i, _i, _p], _i),
+    "ctgpu_backproject_diff_noalloc": ([C.POINTER(Geometry), _i, _i, _s, C.POINTER(Roi), _p, _i,
+                                        _p, _i, _p, _i, _p], _i),
 }
 
 

@@ -32,7 +32,7 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17",
 FILE_FLAGS = {"k_helical.cu": ["--fmad=false"]}
 
 LIB_SOURCES = ["k_common.cu", "k_raysum.cu", "k_filter.cu", "k_backproject.cu", "k_helical.cu",
-               "ctgpu_api.cpp", "filter_design.cpp", "ctsim_api.cpp"]
+               "ctgpu_api.cpp", "filter_design.cpp", "ctsim_api.cpp", "k_noalloc.cu"]
 TOOL_SOURCES = ["tools/ctsimtext.cpp"]
 
 

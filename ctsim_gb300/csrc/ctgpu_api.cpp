@@ -191,6 +191,8 @@ int pitch_for(int nDet) { return (nDet + 3) & ~3; }
 
 }  // namespace
 
+void ctgpu::set_last_error(const char* msg) { g_err = msg; }
+
 // ===========================================================================
 struct ctgpu_phantom {
   std::vector<PElem> elems;   // reference list order: last added first

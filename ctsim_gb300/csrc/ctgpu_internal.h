@@ -79,6 +79,9 @@ constexpr unsigned int kStatusFeatherRange = 2u;
 // status bits written by kernels
 constexpr unsigned int kStatusTimeout = 1u;
 
+// the C ABI's per-thread last-error message (ctgpu_api.cpp)
+void set_last_error(const char* msg);
+
 // device status word (k_common.cu)
 unsigned int* status_pointer();
 cudaError_t status_read_and_clear(unsigned int* value);

@@ -204,6 +204,35 @@ int ctgpu_helical180li(const ctgpu_geometry* g, const float* d_in, int n_view_in
 int ctgpu_halfscan_feather(const ctgpu_geometry* g, float* d_data, int n_view, int pitch,
                            void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Allocation-free variant                                                   */
+/* ------------------------------------------------------------------------ */
+/* No counterpart in the reference.  The "diff" backprojection of
+ * ctgpu_recon_backproject for callers that cannot allocate device memory --
+ * code inside a CUDA-graph capture that must not grow the memory pool,
+ * plug-ins whose host application owns every device allocation, real-time
+ * loops that must not block on the allocator.  It calls no cudaMalloc,
+ * cudaFree or other allocating routine: the per-view steps and per-(view,
+ * column) row ranges the diff backprojector needs live in a fixed 16 MiB
+ * device array inside the library, which every GPU that loads the library
+ * keeps until the process exits.  The caller passes the filtered sinogram
+ * (d_filtered [n_views][filtered_pitch]) and the image (d_image [nx][ny]);
+ * g describes a parallel-beam scan, roi may be NULL; flags: CTGPU_RUN_POSTPROCESS
+ * applies PostProcessing's rotScale, CTGPU_RUN_ACCUMULATE adds to d_image.
+ * Limits: 24*n_views + 16*n_views*nx bytes (+ alignment) must fit in 16 MiB,
+ * about a million view-columns (e.g. 1440 views x 704 columns); larger
+ * requests return CTGPU_ERR_INVALID with the size needed.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All calls
+ * share the array and it keeps the last call's contents (each call rewrites
+ * everything it reads); calls that overlap on the GPU, on different streams
+ * or threads, race on it. */
+int ctgpu_backproject_diff_noalloc(const ctgpu_geometry* g, int nx, int ny,
+                                   const char* interp_name, const ctgpu_roi* roi,
+                                   const float* d_filtered, int filtered_pitch,
+                                   const double* h_view_angles, int n_views, float* d_image,
+                                   int flags, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
