@@ -702,7 +702,7 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
                              bytes, cudaMemcpyHostToDevice, st));
     views = r->d_views;
   }
-  size_t sb = backproject_scratch_bytes(r->bproj, nViews, r->nx);
+  size_t sb = backproject_scratch_bytes(r->bproj, nViews, r->nx, r->ny);
   if (sb) CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
   BackprojLaunch L{};
   L.geometry = r->g.geometry;
