@@ -702,8 +702,6 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
                              bytes, cudaMemcpyHostToDevice, st));
     views = r->d_views;
   }
-  size_t sb = backproject_scratch_bytes(r->bproj, nViews, r->nx, r->ny);
-  if (sb) CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
   BackprojLaunch L{};
   L.geometry = r->g.geometry;
   L.interp = r->interp;
@@ -736,6 +734,8 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
   L.accumulate = accumulate;
   L.outScale = outScale;
   L.status = status_pointer();
+  size_t sb = backproject_scratch_bytes(L);
+  if (sb) CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
   cudaError_t e = launch_backproject_views(L, views, r->d_scratch, st);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "image pixels behind the fan-beam source");

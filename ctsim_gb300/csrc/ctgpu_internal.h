@@ -91,7 +91,7 @@ cudaError_t launch_raysum(const RaysumLaunch& L, cudaStream_t s);
 cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int rowOffset,
                               cudaStream_t s);
 cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
-size_t backproject_scratch_bytes(int bproj, int nViews, int nx, int ny);
+size_t backproject_scratch_bytes(const BackprojLaunch& L);
 cudaError_t launch_backproject_views(const BackprojLaunch& L, const void* views, void* scratch,
                                      cudaStream_t s);
 cudaError_t launch_scale_image(float* image, size_t n, float scale, cudaStream_t s);
