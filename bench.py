@@ -39,17 +39,20 @@ UNIT = "pixel-view updates/s"
 # 4 samples x 4 B gathered per pixel-view update; 30 + 30 FLOP
 BYTES_PER_PV = 16
 FLOP_PER_PV = 60
+# GB300 CUDA cores: 128 FP32 lanes per SM, an FMA counts 2 FLOP
+FP32_LANES_PER_SM = 128
 CONFIG_NAME = ("equiangular 733 det x 720 views (360 deg), 12 random ellipses, abs_hamming 0.54 "
                "FFT zeropad 2, cubic, 512x512 FP32")
 
 
 def peaks():
+    """(HBM GB/s, its source, max SM MHz) from MEASURED_PEAKS.json, else the fallback"""
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return d.get("hbm_gbs", 6800.0), "measured"
-    return 6800.0, "fallback"
+        return d.get("hbm_gbs", 6800.0), "measured", d.get("sm_max_mhz", 2070.0)
+    return 6800.0, "fallback", 2070.0
 
 
 def dist_info():
@@ -91,10 +94,15 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "25"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once the sampler is running
+            t0 = time.time()
+            while not self.rows and time.time() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.start = len(self.rows)
         except OSError:
             self.proc = None
         return self
@@ -114,6 +122,8 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        rows = self.rows[getattr(self, "start", 0):] or self.rows
+        self.rows = rows
         if not self.rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
@@ -178,16 +188,22 @@ def run_reference(args):
     return 0
 
 
-def traffic_per_launch():
-    """DRAM bytes per backprojection launch from the committed ncu summary."""
+def traffic_per_launch(batch):
+    """DRAM bytes (read + write) of one backprojection launch of `batch` slices,
+    from the committed ncu summary of the same kernel (captured at its own
+    batch size; the traffic grows in proportion to the slices)."""
     p = os.path.join(ROOT, "profiles", "backproject_equiangular_cubic_512_ncu.md")
     if not os.path.exists(p):
         return None
+    vals = {}
     with open(p) as f:
         for line in f:
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1])
-    return None
+            for key in ("traffic_bytes_per_launch:", "traffic_batch_slices:"):
+                if line.startswith(key):
+                    vals[key] = float(line.split(":")[1])
+    if "traffic_bytes_per_launch:" not in vals or "traffic_batch_slices:" not in vals:
+        return None
+    return vals["traffic_bytes_per_launch:"] * batch / vals["traffic_batch_slices:"]
 
 
 def run_gpu(args):
@@ -268,28 +284,37 @@ def run_gpu(args):
     cg.sync()
     ray_ms = reduce_max(r0.elapsed_time(r1), world)
 
-    # --- e2e: the C-ABI host-buffer reconstruct call, copies inside ----------------
-    host_sinos = [s[:, :N_DET].cpu().numpy() for s in sinos]
-    for b in range(min(B, 2)):
-        plan.run_host(host_sinos[b], angles[b])
+    # --- e2e: the C-ABI host-buffer batch call, copies inside ---------------------
+    # page-locked host sinograms [B, n_view, n_det] in, images [B, nx, ny] out;
+    # ctgpu_recon_run_batch_host overlaps the copies of one 16-slice chunk with
+    # the reconstruction of the previous one and returns when the images are
+    # in host memory
+    host_sinos = sinos[:, :, :N_DET].contiguous().cpu().pin_memory()
+    host_images = torch.zeros((B, NX, NX), dtype=torch.float32).pin_memory()
+    plan.run_batch_host(host_sinos, angles[0], host_images)
     barrier(world)
+    e2e_steps = max(1, args.steps)
     t0 = time.perf_counter()
-    e2e_steps = max(1, min(args.steps, 5))
     for k in range(e2e_steps):
-        for b in range(B):
-            out = plan.run_host(host_sinos[b], angles[b])
+        plan.run_batch_host(host_sinos, angles[0], host_images)
     e2e_s = reduce_max(time.perf_counter() - t0, world)
-    # parity spot check of the last slice against the device path
-    dev_img = images[B - 1].cpu().numpy()
-    e2e_err = float(np.linalg.norm(out - dev_img) / np.linalg.norm(dev_img))
+    # parity spot check against the device path, and of the per-slice host call
+    dev_imgs = images.cpu().numpy()
+    e2e_err = float(np.linalg.norm(host_images.numpy() - dev_imgs) / np.linalg.norm(dev_imgs))
+    one = plan.run_host(host_sinos[B - 1].numpy(), angles[B - 1])
+    single_err = float(np.linalg.norm(one - dev_imgs[B - 1]) / np.linalg.norm(dev_imgs[B - 1]))
 
     if rank != 0:
         return 0
     steps = args.steps
     total_pv = PV_PER_SLICE * B * steps * world
     value = total_pv / (fbp_ms / 1e3)
-    hbm, src = peaks()
-    achieved = BYTES_PER_PV * PV_PER_SLICE * B / (bp_avg_ms / 1e3) / 1e9
+    hbm, src, sm_mhz = peaks()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = sms * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    bp_s = bp_avg_ms / 1e3
+    flops = FLOP_PER_PV * PV_PER_SLICE * B
+    traffic = traffic_per_launch(B)
     cpu_v, cpu_sample, cpu_threads = cpu_fbp_rate(seed=7, seconds=args.cpu_seconds,
                                                   views=args.ref_views)
     line = {
@@ -303,20 +328,34 @@ def run_gpu(args):
         "raysums": {"metric": "ray-sums/s", "value": RAYS_PER_SLICE * B * steps * world / (ray_ms / 1e3),
                     "ms_per_step": ray_ms / steps,
                     "ray_element_pairs_per_s": RAYS_PER_SLICE * 12 * B * steps * world / (ray_ms / 1e3)},
-        "roofline": {"kernel": "backproject_table_kernel<equiangular,cubic>", "bound": "hbm",
-                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": src, "traffic": traffic_per_launch(),
-                     "algorithmic_bytes_per_launch": BYTES_PER_PV * PV_PER_SLICE * B,
+        "roofline": {"kernel": "backproject_table_kernel<equiangular,cubic>", "bound": "fp32",
+                     "achieved": flops / bp_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": flops / bp_s / 1e12 / fp32_peak,
+                     "peak_source": "nominal FP32 of %d SMs x %d lanes x 2 FLOP x %.0f MHz "
+                                    "(max SM clock); MEASURED_PEAKS.json holds no FP32 figure"
+                                    % (sms, FP32_LANES_PER_SM, sm_mhz),
+                     "traffic": traffic,
+                     "algorithmic_flops_per_launch": flops, "flop_per_pixel_view": FLOP_PER_PV,
                      "avg_launch_ms": bp_avg_ms, "slices_per_launch": B,
-                     "fp32_tflops": FLOP_PER_PV * PV_PER_SLICE * B / (bp_avg_ms / 1e3) / 1e12},
+                     "hbm": {"achieved_gbs": traffic / bp_s / 1e9 if traffic else None,
+                             "peak_gbs": hbm, "peak_source": src,
+                             "frac": traffic / bp_s / 1e9 / hbm if traffic else None},
+                     "gather": {"bytes_per_pixel_view": BYTES_PER_PV,
+                                "achieved_gbs": BYTES_PER_PV * PV_PER_SLICE * B / bp_s / 1e9,
+                                "served_from": "shared memory"}},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                          "sample": cpu_sample},
         "e2e": {"value": PV_PER_SLICE * B * e2e_steps * world / e2e_s, "unit": UNIT,
-                "h2d_bytes_per_step": B * (N_VIEW * N_DET * 4 + N_VIEW * 8),
+                "h2d_bytes_per_step": B * N_VIEW * N_DET * 4 + ((B + 15) // 16) * N_VIEW * 8,
                 "d2h_bytes_per_step": B * NX * NX * 4,
-                "steps": e2e_steps, "path": "ctgpu_recon_run_host (pageable host buffers)",
-                "parity_vs_device_rel_l2": e2e_err},
-        "gpu_launches": steps * (B + 1),
+                "steps": e2e_steps, "ms_per_step": e2e_s / e2e_steps * 1e3,
+                "path": "ctgpu_recon_run_batch_host (page-locked host buffers, 16-slice chunks, "
+                        "copies overlapped with compute)",
+                "parity_vs_device_rel_l2": e2e_err,
+                "single_slice_run_host_rel_l2": single_err},
+        # per step: one filter launch per slice; interval rows, tile records and
+        # the backprojection itself for the batch
+        "gpu_launches": steps * (B + 3),
         "clocks": clk.summary(),
     }
     print(json.dumps(line))

@@ -254,10 +254,22 @@ struct ctgpu_recon {
   size_t d_sino_cap = 0;
   float* d_image = nullptr;
   size_t d_image_cap = 0;
+  // run_batch_host: two chunk buffers each, copy / compute streams and events
+  float* d_bsino = nullptr;
+  size_t d_bsino_cap = 0;
+  float* d_bimage = nullptr;
+  size_t d_bimage_cap = 0;
+  cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
+  cudaEvent_t ev[6] = {};   // in_done[2], comp_done[2], out_done[2]
   ~ctgpu_recon() {
     for (void* p : {(void*)d_taps, (void*)d_weights, (void*)d_filtered, (void*)d_angles,
-                    (void*)d_views, (void*)d_scratch, (void*)d_sino, (void*)d_image})
+                    (void*)d_views, (void*)d_scratch, (void*)d_sino, (void*)d_image,
+                    (void*)d_bsino, (void*)d_bimage})
       if (p) cudaFree(p);
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    for (cudaStream_t s : {s_in, s_comp, s_out})
+      if (s) cudaStreamDestroy(s);
   }
 };
 
@@ -833,6 +845,59 @@ int ctgpu_recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int 
   if (post && r->bproj != kTrig) scale = (float)(scale * r->rotScale);
   return recon_backproject_scaled(r, r->d_filtered, r->pitch, h_angles, nView, d_images, 0, scale,
                                   st, nBatch, fStride, (size_t)imageSliceStride);
+}
+
+int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
+                               const double* h_angles, float* h_images, int flags) {
+  if (!r || !h_sinos || !h_angles || !h_images) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (nBatch < 1) return fail(CTGPU_ERR_INVALID, "batch size must be >= 1");
+  if (flags & CTGPU_RUN_ACCUMULATE) return fail(CTGPU_ERR_UNSUPPORTED, "batched runs overwrite their images");
+  const int nDet = r->g.n_det, nView = r->g.n_view;
+  const int chunk = nBatch < 16 ? nBatch : 16;
+  const size_t sStride = (size_t)nView * r->pitch, iStride = (size_t)r->nx * r->ny;
+  CUDA_TRY(ensure_device(r->d_bsino, r->d_bsino_cap, 2 * chunk * sStride));
+  CUDA_TRY(ensure_device(r->d_bimage, r->d_bimage_cap, 2 * chunk * iStride));
+  for (cudaStream_t* s : {&r->s_in, &r->s_comp, &r->s_out})
+    if (!*s) CUDA_TRY(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking));
+  for (cudaEvent_t& e : r->ev)
+    if (!e) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaEvent_t* inDone = r->ev;
+  cudaEvent_t* compDone = r->ev + 2;
+  cudaEvent_t* outDone = r->ev + 4;
+  const int nChunks = (nBatch + chunk - 1) / chunk;
+  // image copy of chunk c, issued one iteration late so that a pageable
+  // destination (whose copy blocks the host) does not hold back the next
+  // chunk's input copy and launch
+  auto copy_out = [&](int c) -> int {
+    const int b = c & 1, n = nBatch - c * chunk < chunk ? nBatch - c * chunk : chunk;
+    CUDA_TRY(cudaStreamWaitEvent(r->s_out, compDone[b], 0));
+    CUDA_TRY(cudaMemcpyAsync(h_images + (size_t)c * chunk * iStride, r->d_bimage + b * chunk * iStride,
+                             sizeof(float) * iStride * n, cudaMemcpyDeviceToHost, r->s_out));
+    CUDA_TRY(cudaEventRecord(outDone[b], r->s_out));
+    return CTGPU_OK;
+  };
+  for (int c = 0; c < nChunks; c++) {
+    const int b = c & 1, n = nBatch - c * chunk < chunk ? nBatch - c * chunk : chunk;
+    float* dS = r->d_bsino + b * chunk * sStride;
+    float* dI = r->d_bimage + b * chunk * iStride;
+    if (c >= 2) CUDA_TRY(cudaStreamWaitEvent(r->s_in, compDone[b], 0));   // buffer b read
+    CUDA_TRY(cudaMemcpy2DAsync(dS, sizeof(float) * r->pitch,
+                               h_sinos + (size_t)c * chunk * nView * nDet, sizeof(float) * nDet,
+                               sizeof(float) * nDet, (size_t)n * nView, cudaMemcpyHostToDevice,
+                               r->s_in));
+    CUDA_TRY(cudaEventRecord(inDone[b], r->s_in));
+    CUDA_TRY(cudaStreamWaitEvent(r->s_comp, inDone[b], 0));
+    if (c >= 2) CUDA_TRY(cudaStreamWaitEvent(r->s_comp, outDone[b], 0));   // image b copied out
+    int rc = ctgpu_recon_run_batch(r, n, dS, r->pitch, (long long)sStride, h_angles, dI,
+                                   (long long)iStride, flags & CTGPU_RUN_POSTPROCESS, r->s_comp);
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(compDone[b], r->s_comp));
+    if (c >= 1 && (rc = copy_out(c - 1))) return rc;
+  }
+  int rc = copy_out(nChunks - 1);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(r->s_out));
+  return ctgpu_sync(r->s_comp);
 }
 
 int ctgpu_recon_backproject_batch(ctgpu_recon* r, int nBatch, const float* d_filtered, int pitch,

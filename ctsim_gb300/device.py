@@ -131,6 +131,32 @@ class ReconPlan:
                                          out.ctypes.data_as(C.c_void_p)))
         return out
 
+    def run_batch_host(self, sinos, angles, out=None, postprocess=True):
+        """run_batch with host buffers: sinos [B, n_view, n_det] (numpy array or
+        CPU tensor, ideally page-locked), images returned in `out` [B, nx, ny]
+        (allocated as numpy if None).  Copies overlap the reconstruction."""
+        def host_ptr(x, dtype):
+            if hasattr(x, "data_ptr"):
+                if x.is_cuda or not x.is_contiguous():
+                    raise ValueError("host buffers must be contiguous CPU tensors")
+                return C.c_void_p(x.data_ptr())
+            if x.dtype != dtype or not x.flags.c_contiguous:
+                raise ValueError("host buffers must be contiguous %s arrays" % np.dtype(dtype))
+            return x.ctypes.data_as(C.c_void_p)
+        B = sinos.shape[0]
+        if tuple(sinos.shape[1:]) != (self.geometry.n_view, self.geometry.n_det):
+            raise ValueError("sinos must be [B, n_view, n_det]")
+        if out is None:
+            out = np.zeros((B, self.nx, self.ny), np.float32)
+        if tuple(out.shape) != (B, self.nx, self.ny):
+            raise ValueError("out must be [B, nx, ny]")
+        ang = np.ascontiguousarray(angles, np.float64)
+        check(lib().ctgpu_recon_run_batch_host(self._h, B, host_ptr(sinos, np.float32),
+                                               ang.ctypes.data_as(C.c_void_p),
+                                               host_ptr(out, np.float32),
+                                               RUN_POSTPROCESS if postprocess else 0))
+        return out
+
     def project(self, image, angles, out, scale=1.0, stream=None):
         ang = np.ascontiguousarray(angles, np.float64)
         check(lib().ctgpu_recon_project(self._h, _ptr(image), ang.ctypes.data_as(C.c_void_p),

@@ -172,6 +172,15 @@ int ctgpu_recon_run_batch(ctgpu_recon* r, int n_batch, const float* d_sinos, int
                           long long sino_slice_stride, const double* h_view_angles,
                           float* d_images, long long image_slice_stride, int flags,
                           void* stream);
+/* ctgpu_recon_run_batch with host buffers: h_sinos n_batch sinograms
+ * [n_view][n_det] back to back, h_images n_batch images [nx][ny] back to back.
+ * Slices move in chunks of up to 16 through two device buffers, so the copy
+ * of one chunk overlaps the reconstruction of the previous one (page-locked
+ * host buffers make the copies asynchronous; pageable ones work, with less
+ * overlap).  Synchronous: returns when h_images is written.  No reference
+ * counterpart (CTSim reconstructs one slice per Reconstructor). */
+int ctgpu_recon_run_batch_host(ctgpu_recon* r, int n_batch, const float* h_sinos,
+                               const double* h_view_angles, float* h_images, int flags);
 /* Backprojection of n_batch filtered sinograms (same geometry and angles) in
  * one launch; flags: CTGPU_RUN_POSTPROCESS folds PostProcessing in. */
 int ctgpu_recon_backproject_batch(ctgpu_recon* r, int n_batch, const float* d_filtered,

@@ -254,3 +254,37 @@ def test_batched_launch_equals_single(gpu, geo, interp, bp):
         plan.run(sinos[b], angs, single)
         cg.sync()
         assert rel_l2(out[b].cpu().numpy(), single.cpu().numpy()) < 1e-6
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_batch_host_equals_device_batch(gpu, pinned):
+    """ctgpu_recon_run_batch_host (chunks of 16, copies overlapped) gives the
+    device batch's images; 37 slices = two full chunks and a ragged one."""
+    torch, cg, device = gpu
+    from ctsim_gb300 import phantoms
+    B, nd, nv, n = 37, 129, 90, 64
+    sinos, angs = [], None
+    for b in range(B):
+        ph = phantoms.make_phantom(phantoms.random_ellipses(seed=300 + b, n=5))
+        sc = cg.Scanner(ph, "equiangular", nd, nv)
+        s = device.alloc_sinogram(nv, nd)
+        angs = device.raysums(sc, ph, s)
+        sinos.append(s)
+    g = sc.geometry()
+    plan = device.ReconPlan(g, n, n, "abs_hamming", 0.54, "fft", 2, "direct", "cubic", 1, "table")
+    batch = torch.stack(sinos)
+    ref = torch.zeros((B, n, n), device="cuda")
+    plan.run_batch(batch, angs, ref)
+    cg.sync()
+    host = batch[:, :, :nd].contiguous().cpu()
+    if pinned:
+        host = host.pin_memory()
+        out = torch.zeros((B, n, n), dtype=torch.float32).pin_memory()
+    else:
+        host = host.numpy()
+        out = None
+    res = plan.run_batch_host(host, angs, out)
+    res = res.numpy() if hasattr(res, "numpy") else res
+    r = ref.cpu().numpy()
+    for b in range(B):
+        assert rel_l2(res[b], r[b]) < 1e-7, b
