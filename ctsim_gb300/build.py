@@ -30,6 +30,9 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17",
 # per-file device flags: the helical weights are FP64 expressions the
 # reference evaluates without fused multiply-adds
 FILE_FLAGS = {"k_helical.cu": ["--fmad=false"]}
+# extra nvcc flags for every translation unit, e.g. tuning macros
+# (CTGPU_NVCC_FLAGS="-DCTGPU_BP_CTAS_PER_SM=5")
+EXTRA_FLAGS = os.environ.get("CTGPU_NVCC_FLAGS", "").split()
 
 LIB_SOURCES = ["k_common.cu", "k_raysum.cu", "k_filter.cu", "k_backproject.cu", "k_helical.cu",
                "ctgpu_api.cpp", "filter_design.cpp", "ctsim_api.cpp", "k_noalloc.cu"]
@@ -60,7 +63,8 @@ def _compile(src, force):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if not force and not _stale(obj, [src] + _headers()):
         return obj, None
-    cmd = [nvcc()] + NVFLAGS + FILE_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + NVFLAGS + EXTRA_FLAGS + FILE_FLAGS.get(os.path.basename(src), []) + \
+        ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         return obj, "%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr)
