@@ -240,7 +240,8 @@ struct ctgpu_recon {
   int iDetCenter, pitch;
   double xMin, xMax, yMin, yMax, xInc, yInc, rotScale, startR, startPhi;
   FilterDesign fd;
-  float* d_taps = nullptr;
+  int fftN = 0;
+  float* d_spec = nullptr;   // FilterSpectrum::spectrum, then ::twiddle
   float* d_weights = nullptr;
   float* d_filtered = nullptr;
   size_t d_filtered_cap = 0;
@@ -262,7 +263,7 @@ struct ctgpu_recon {
   cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
   cudaEvent_t ev[6] = {};   // in_done[2], comp_done[2], out_done[2]
   ~ctgpu_recon() {
-    for (void* p : {(void*)d_taps, (void*)d_weights, (void*)d_filtered, (void*)d_angles,
+    for (void* p : {(void*)d_spec, (void*)d_weights, (void*)d_filtered, (void*)d_angles,
                     (void*)d_views, (void*)d_scratch, (void*)d_sino, (void*)d_image,
                     (void*)d_bsino, (void*)d_bimage})
       if (p) cudaFree(p);
@@ -626,10 +627,15 @@ int ctgpu_recon_create(const ctgpu_geometry* g, int nx, int ny, const char* filt
   double x0 = r->xMin + r->xInc / 2, y0 = r->yMin + r->yInc / 2;
   r->startR = std::sqrt(x0 * x0 + y0 * y0);
   r->startPhi = std::atan2(y0, x0);
-  size_t nt = r->fd.taps.size(), nw = r->fd.weights.size(), c1 = 0, c2 = 0;
-  cudaError_t e = ensure_device(r->d_taps, c1, nt);
+  FilterSpectrum fs;
+  filter_spectrum(r->fd, g->n_det, fs);
+  r->fftN = fs.fftN;
+  const size_t ns = fs.spectrum.size(), nw = r->fd.weights.size();
+  size_t c1 = 0, c2 = 0;
+  cudaError_t e = ensure_device(r->d_spec, c1, 2 * ns);
   if (e == cudaSuccess) e = ensure_device(r->d_weights, c2, nw);
-  if (e == cudaSuccess) e = cudaMemcpy(r->d_taps, r->fd.taps.data(), sizeof(float) * nt, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(r->d_spec, fs.spectrum.data(), sizeof(float) * ns, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(r->d_spec + ns, fs.twiddle.data(), sizeof(float) * ns, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(r->d_weights, r->fd.weights.data(), sizeof(float) * nw, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     delete r;
@@ -648,23 +654,37 @@ int ctgpu_recon_image_axes(const ctgpu_recon* r, double extent[4], double increm
 
 void ctgpu_recon_destroy(ctgpu_recon* r) { delete r; }
 
-int ctgpu_recon_filter(ctgpu_recon* r, const float* d_sino, int sinoPitch, int nViews,
-                       float* d_filtered, int filtPitch, void* stream) {
-  if (!r || !d_sino || !d_filtered) return fail(CTGPU_ERR_INVALID, "null argument");
-  if (sinoPitch < r->g.n_det || filtPitch < r->g.n_det) return fail(CTGPU_ERR_INVALID, "pitch < nDet");
+// Filtering of nBatch sinograms of nViews rows each, one launch.
+static int recon_filter_batch(ctgpu_recon* r, const float* d_sino, int sinoPitch,
+                              size_t sinoStride, int nViews, float* d_filtered, int filtPitch,
+                              size_t filtStride, int nBatch, cudaStream_t st) {
   FilterLaunch L{};
   L.nDet = r->g.n_det;
   L.nViews = nViews;
   L.inPitch = sinoPitch;
   L.outPitch = filtPitch;
-  L.taps = r->d_taps;
+  L.fftN = r->fftN;
+  L.spectrum = reinterpret_cast<const float2*>(r->d_spec);
+  L.twiddle = reinterpret_cast<const float2*>(r->d_spec) + r->fftN;
   L.weights = r->d_weights;
   L.in = d_sino;
   L.out = d_filtered;
-  cudaError_t e = launch_filter(L, (cudaStream_t)stream);
-  if (e == cudaErrorInvalidValue) return fail(CTGPU_ERR_UNSUPPORTED, "nDet too large for the shared-memory filter");
+  L.nBatch = nBatch;
+  L.inSliceStride = sinoStride;
+  L.outSliceStride = filtStride;
+  cudaError_t e = launch_filter(L, st);
+  if (e == cudaErrorInvalidValue)
+    return fail(CTGPU_ERR_UNSUPPORTED, "nDet too large for the shared-memory FFT filter (at most 8192)");
   CUDA_TRY(e);
   return ok();
+}
+
+int ctgpu_recon_filter(ctgpu_recon* r, const float* d_sino, int sinoPitch, int nViews,
+                       float* d_filtered, int filtPitch, void* stream) {
+  if (!r || !d_sino || !d_filtered) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (sinoPitch < r->g.n_det || filtPitch < r->g.n_det) return fail(CTGPU_ERR_INVALID, "pitch < nDet");
+  return recon_filter_batch(r, d_sino, sinoPitch, 0, nViews, d_filtered, filtPitch, 0, 1,
+                            (cudaStream_t)stream);
 }
 
 // Backprojection of nViews filtered rows; outScale multiplies this launch's sum.
@@ -828,18 +848,9 @@ int ctgpu_recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int 
   cudaStream_t st = (cudaStream_t)stream;
   size_t fStride = (size_t)nView * r->pitch;
   CUDA_TRY(ensure_device(r->d_filtered, r->d_filtered_cap, fStride * nBatch));
-  FilterLaunch F{};
-  F.nDet = r->g.n_det;
-  F.nViews = nView;
-  F.inPitch = sinoPitch;
-  F.outPitch = r->pitch;
-  F.taps = r->d_taps;
-  F.weights = r->d_weights;
-  for (int b = 0; b < nBatch; b++) {
-    F.in = d_sinos + (size_t)b * sinoSliceStride;
-    F.out = r->d_filtered + fStride * b;
-    CUDA_TRY(launch_filter(F, st));
-  }
+  int rc = recon_filter_batch(r, d_sinos, sinoPitch, (size_t)sinoSliceStride, nView,
+                              r->d_filtered, r->pitch, fStride, nBatch, st);
+  if (rc) return rc;
   float scale = raw_scale(r);
   bool post = (flags & CTGPU_RUN_POSTPROCESS) != 0;
   if (post && r->bproj != kTrig) scale = (float)(scale * r->rotScale);

@@ -44,10 +44,14 @@ struct RaysumLaunch {
 // Filter: out[v][n] = sum_i (w[i] * in[v][i]) * taps[n - i + nDet - 1]
 struct FilterLaunch {
   int nDet, nViews, inPitch, outPitch;
-  const float* taps;      // 2*nDet - 1
-  const float* weights;   // nDet (fan pre-weighting, 1 for parallel)
-  const float* in;
-  float* out;
+  int fftN;                 // circular convolution length (power of two >= 2*nDet-1)
+  const float2* spectrum;   // fftN: DFT of the filter kernel / fftN
+  const float2* twiddle;    // fftN: exp(-2 pi i m / fftN)
+  const float* weights;     // nDet (fan pre-weighting, 1 for parallel)
+  const float* in;          // [nBatch][nViews][inPitch]
+  float* out;               // [nBatch][nViews][outPitch]
+  int nBatch;
+  size_t inSliceStride, outSliceStride;
 };
 
 // Backprojection of one problem.

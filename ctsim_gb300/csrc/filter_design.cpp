@@ -373,8 +373,49 @@ bool design_filter(const FilterSpec& sp, FilterDesign& out, std::string& err) {
     }
   }
   out.taps.assign(taps.begin(), taps.end());
+  out.taps64 = taps;
   out.weights.assign(w.begin(), w.end());
   return true;
+}
+
+// In-place FP64 radix-2 FFT (decimation in time, bit-reversed input order),
+// forward sign; n a power of two.
+static void fft64(std::vector<std::complex<double>>& a) {
+  const size_t n = a.size();
+  for (size_t i = 1, j = 0; i < n; i++) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) std::swap(a[i], a[j]);
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    const double ang = -2.0 * PI / (double)len;
+    for (size_t i = 0; i < n; i += len)
+      for (size_t k = 0; k < len / 2; k++) {
+        const std::complex<double> w(std::cos(ang * k), std::sin(ang * k));
+        const std::complex<double> u = a[i + k], v = a[i + k + len / 2] * w;
+        a[i + k] = u + v;
+        a[i + k + len / 2] = u - v;
+      }
+  }
+}
+
+void filter_spectrum(const FilterDesign& d, int nDet, FilterSpectrum& out) {
+  int N = 1;
+  while (N < 2 * nDet - 1) N <<= 1;
+  std::vector<std::complex<double>> k(N, 0.0);
+  for (int m = -(nDet - 1); m < nDet; m++) k[m >= 0 ? m : N + m] = d.taps64[m + nDet - 1];
+  fft64(k);
+  out.fftN = N;
+  out.spectrum.resize(2 * (size_t)N);
+  out.twiddle.resize(2 * (size_t)N);
+  for (int f = 0; f < N; f++) {
+    out.spectrum[2 * f] = (float)(k[f].real() / N);
+    out.spectrum[2 * f + 1] = (float)(k[f].imag() / N);
+    const double a = -2.0 * PI * (double)f / (double)N;
+    out.twiddle[2 * f] = (float)std::cos(a);
+    out.twiddle[2 * f + 1] = (float)std::sin(a);
+  }
 }
 
 }  // namespace ctgpu
