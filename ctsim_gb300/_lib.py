@@ -37,6 +37,19 @@ class Roi(C.Structure):
                 ("y_max", C.c_double)]
 
 
+class BatchProblem(C.Structure):
+    """ctgpu_batch_problem"""
+    _fields_ = [("geometry", Geometry), ("nx", C.c_int), ("ny", C.c_int),
+                ("filter_name", C.c_char_p), ("filter_param", C.c_double),
+                ("filter_method", C.c_char_p), ("zeropad", C.c_int),
+                ("filter_generation", C.c_char_p), ("interp_name", C.c_char_p),
+                ("backproj_name", C.c_char_p), ("d_sino", C.c_void_p), ("sino_pitch", C.c_int),
+                ("h_view_angles", C.c_void_p), ("d_image", C.c_void_p)]
+
+
+BATCH_AUTOTUNE = 1
+BATCH_GRAPH = 2
+
 _lib = None
 
 # (name, argtypes) for every exported entry point; used for loading and for
@@ -75,6 +88,10 @@ SIGNATURES = {
     "ctgpu_helical180li_size": ([C.POINTER(Geometry), _i, _i, C.POINTER(_i)], _i),
     "ctgpu_helical180li": ([C.POINTER(Geometry), _p, _i, _i, _p, _i, _p, C.POINTER(_i), _p], _i),
     "ctgpu_halfscan_feather": ([C.POINTER(Geometry), _p, _i, _i, _p], _i),
+    "ctgpu_batch_create": ([C.POINTER(BatchProblem), _i, _i, _pp], _i),
+    "ctgpu_batch_run": ([_p, _p], _i),
+    "ctgpu_batch_shape": ([_p, C.POINTER(_i), C.POINTER(_i)], _i),
+    "ctgpu_batch_destroy": ([_p], None),
     "ctgpu_backproject_diff_noalloc": ([C.POINTER(Geometry), _i, _i, _s, C.POINTER(Roi), _p, _i,
                                         _p, _i, _p, _i, _p], _i),
 }

@@ -6,8 +6,10 @@
 // points, filter design, fixed-point backprojection steps), and launches the
 // sm_103a kernels for everything that is per ray, per detector sample or per
 // pixel.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <memory>
 #include <cstring>
 #include <string>
 #include <strings.h>
@@ -687,6 +689,47 @@ int ctgpu_recon_filter(ctgpu_recon* r, const float* d_sino, int sinoPitch, int n
                             (cudaStream_t)stream);
 }
 
+// The backprojection launch descriptor of a plan (Backproject::Backproject's
+// grid and geometry, backprojectors.cpp:264-319).
+static BackprojLaunch make_launch(const ctgpu_recon* r, int nViews, int pitch,
+                                  const double* d_angles, const float* d_filtered,
+                                  float* d_image, int accumulate, float outScale, int nBatch,
+                                  size_t filtStride, size_t imageStride) {
+  BackprojLaunch L{};
+  L.geometry = r->g.geometry;
+  L.interp = r->interp;
+  L.bproj = r->bproj;
+  L.nDet = r->g.n_det;
+  L.nx = r->nx;
+  L.ny = r->ny;
+  L.nViews = nViews;
+  L.pitch = pitch;
+  L.iDetCenter = r->iDetCenter;
+  L.detInc = r->g.det_inc;
+  L.xMin = r->xMin;
+  L.yMin = r->yMin;
+  L.xInc = r->xInc;
+  L.yInc = r->yInc;
+  L.focalLength = r->g.focal_length;
+  L.sdl = r->g.source_detector_length;
+  L.rotScale = r->rotScale;
+  {
+    double xm = std::fmax(std::fabs(r->xMin), std::fabs(r->xMax));
+    double ym = std::fmax(std::fabs(r->yMin), std::fabs(r->yMax));
+    L.minSourceDist = r->g.focal_length - std::sqrt(xm * xm + ym * ym);
+  }
+  L.angles = d_angles;
+  L.filtered = d_filtered;
+  L.image = d_image;
+  L.nBatch = nBatch;
+  L.filtSliceStride = filtStride;
+  L.imageSliceStride = imageStride;
+  L.accumulate = accumulate;
+  L.outScale = outScale;
+  L.status = status_pointer();
+  return L;
+}
+
 // Backprojection of nViews filtered rows; outScale multiplies this launch's sum.
 static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int pitch,
                                     const double* h_angles, int nViews, float* d_image,
@@ -734,38 +777,8 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
                              bytes, cudaMemcpyHostToDevice, st));
     views = r->d_views;
   }
-  BackprojLaunch L{};
-  L.geometry = r->g.geometry;
-  L.interp = r->interp;
-  L.bproj = r->bproj;
-  L.nDet = r->g.n_det;
-  L.nx = r->nx;
-  L.ny = r->ny;
-  L.nViews = nViews;
-  L.pitch = pitch;
-  L.iDetCenter = r->iDetCenter;
-  L.detInc = r->g.det_inc;
-  L.xMin = r->xMin;
-  L.yMin = r->yMin;
-  L.xInc = r->xInc;
-  L.yInc = r->yInc;
-  L.focalLength = r->g.focal_length;
-  L.sdl = r->g.source_detector_length;
-  L.rotScale = r->rotScale;
-  {
-    double xm = std::fmax(std::fabs(r->xMin), std::fabs(r->xMax));
-    double ym = std::fmax(std::fabs(r->yMin), std::fabs(r->yMax));
-    L.minSourceDist = r->g.focal_length - std::sqrt(xm * xm + ym * ym);
-  }
-  L.angles = r->d_angles;
-  L.filtered = d_filtered;
-  L.image = d_image;
-  L.nBatch = nBatch;
-  L.filtSliceStride = filtStride;
-  L.imageSliceStride = imageStride;
-  L.accumulate = accumulate;
-  L.outScale = outScale;
-  L.status = status_pointer();
+  BackprojLaunch L = make_launch(r, nViews, pitch, r->d_angles, d_filtered, d_image, accumulate,
+                                 outScale, nBatch, filtStride, imageStride);
   size_t sb = backproject_scratch_bytes(L);
   if (sb) CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
   cudaError_t e = launch_backproject_views(L, views, r->d_scratch, st);
@@ -1048,5 +1061,275 @@ int ctgpu_halfscan_feather(const ctgpu_geometry* g, float* d_data, int nView, in
   CUDA_TRY(e);
   return ok();
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched reconstruction of problems of uneven sizes.  Each problem keeps a
+// plan of its own (filter design, image grid, geometry); the set-up launches
+// of the problems (filter, interval rows, tile records) run as parallel
+// branches on kSideStreams streams, then one persistent launch backprojects
+// every (problem, tile) item, longest first.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kSideStreams = 4;
+
+struct BatchEntry {
+  ctgpu_recon* plan = nullptr;
+  const float* d_sino = nullptr;
+  int sinoPitch = 0;
+  float* d_image = nullptr;
+  size_t filtOff = 0, angOff = 0, scratchOff = 0;   // arena offsets
+  BackprojLaunch L{};
+  TablePrep prep{};
+};
+
+}  // namespace
+
+struct ctgpu_batch {
+  std::vector<BatchEntry> probs;
+  std::vector<BatchItem> items;
+  unsigned char* d_arena = nullptr;
+  size_t arenaBytes = 0;
+  BatchProblem* d_probs = nullptr;
+  BatchItem* d_items = nullptr;
+  int* d_counter = nullptr;
+  int flags = 0;
+  bool shaped = false;
+  BatchShape shape{4, 16};
+  int gridBlocks = 0;
+  cudaStream_t side[kSideStreams] = {};
+  cudaStream_t capture = nullptr;
+  cudaEvent_t fork = nullptr, join[kSideStreams] = {};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~ctgpu_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (auto& e : probs)
+      if (e.plan) ctgpu_recon_destroy(e.plan);
+    for (void* p : {(void*)d_arena, (void*)d_probs, (void*)d_items, (void*)d_counter})
+      if (p) cudaFree(p);
+    if (fork) cudaEventDestroy(fork);
+    for (cudaEvent_t e : join)
+      if (e) cudaEventDestroy(e);
+    for (cudaStream_t s : side)
+      if (s) cudaStreamDestroy(s);
+    if (capture) cudaStreamDestroy(capture);
+  }
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// problem table for a launch shape; false when a problem's window does not fit
+static bool batch_table(const ctgpu_batch* b, const BatchShape& shape,
+                        std::vector<BatchProblem>& out) {
+  out.resize(b->probs.size());
+  for (size_t i = 0; i < b->probs.size(); i++) {
+    const BatchEntry& e = b->probs[i];
+    BatchProblem& P = out[i];
+    P.L = e.L;
+    P.recs = b->d_arena + e.scratchOff;
+    P.rows = b->d_arena + e.scratchOff + e.prep.recBytes;
+    P.kind = e.prep.kind;
+    P.win = e.prep.win;
+    P.rpitch = e.prep.rpitch;
+    P.elemBytes = e.prep.elemBytes;
+    P.eps = e.prep.eps;
+    P.tilesX = (e.L.nx + 31) / 32;
+    P.cv = batch_views_per_stage(e.prep, shape);
+    if (P.cv < 1) return false;
+  }
+  return true;
+}
+
+// the problems' set-up launches as branches forked from and joined to s
+static int batch_enqueue_prep(ctgpu_batch* b, cudaStream_t s) {
+  CUDA_TRY(cudaEventRecord(b->fork, s));
+  for (int k = 0; k < kSideStreams; k++) CUDA_TRY(cudaStreamWaitEvent(b->side[k], b->fork, 0));
+  for (size_t i = 0; i < b->probs.size(); i++) {
+    BatchEntry& e = b->probs[i];
+    cudaStream_t ss = b->side[i % kSideStreams];
+    int rc = recon_filter_batch(e.plan, e.d_sino, e.sinoPitch, 0, e.L.nViews,
+                                reinterpret_cast<float*>(b->d_arena + e.filtOff), e.plan->pitch,
+                                0, 1, ss);
+    if (rc) return rc;
+    CUDA_TRY(launch_table_prep(e.L, e.prep, b->d_arena + e.scratchOff, ss));
+  }
+  for (int k = 0; k < kSideStreams; k++) {
+    CUDA_TRY(cudaEventRecord(b->join[k], b->side[k]));
+    CUDA_TRY(cudaStreamWaitEvent(s, b->join[k], 0));
+  }
+  return ok();
+}
+
+static int batch_enqueue_backprojection(ctgpu_batch* b, cudaStream_t s) {
+  CUDA_TRY(cudaMemsetAsync(b->d_counter, 0, sizeof(int), s));
+  CUDA_TRY(launch_backproject_batch(b->d_probs, b->d_items, (int)b->items.size(), b->d_counter,
+                                    b->shape, b->gridBlocks, status_pointer(), s));
+  return ok();
+}
+
+static int batch_set_shape(ctgpu_batch* b, const BatchShape& shape) {
+  std::vector<BatchProblem> table;
+  if (!batch_table(b, shape, table)) return fail(CTGPU_ERR_UNSUPPORTED, "shape does not fit");
+  CUDA_TRY(prepare_backproject_batch(shape, &b->gridBlocks));
+  CUDA_TRY(cudaMemcpy(b->d_probs, table.data(), sizeof(BatchProblem) * table.size(),
+                      cudaMemcpyHostToDevice));
+  b->shape = shape;
+  return ok();
+}
+
+// Autotuner: every candidate launch shape that fits is timed on this batch
+// (prepared data, one warm-up and two timed launches, the faster kept) and
+// the fastest is kept.
+static int batch_tune(ctgpu_batch* b, cudaStream_t s) {
+  static const BatchShape cands[] = {{4, 16}, {4, 8}, {3, 16}, {2, 16}};
+  cudaEvent_t t0, t1;
+  CUDA_TRY(cudaEventCreate(&t0));
+  CUDA_TRY(cudaEventCreate(&t1));
+  float best = 1e30f;
+  BatchShape bestShape{0, 0};
+  int rc = ok();
+  for (const BatchShape& c : cands) {
+    if (batch_set_shape(b, c) != CTGPU_OK) continue;
+    float ms = 1e30f;
+    for (int rep = 0; rep < 3 && rc == CTGPU_OK; rep++) {
+      if (cudaEventRecord(t0, s) != cudaSuccess) rc = fail(CTGPU_ERR_CUDA, "event");
+      if (rc == CTGPU_OK) rc = batch_enqueue_backprojection(b, s);
+      if (rc == CTGPU_OK && cudaEventRecord(t1, s) != cudaSuccess) rc = fail(CTGPU_ERR_CUDA, "event");
+      if (rc == CTGPU_OK) rc = ctgpu_sync(s);
+      float t = 0.f;
+      if (rc == CTGPU_OK && rep > 0 && cudaEventElapsedTime(&t, t0, t1) == cudaSuccess && t < ms)
+        ms = t;
+    }
+    if (rc != CTGPU_OK) break;
+    if (ms < best) {
+      best = ms;
+      bestShape = c;
+    }
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (rc != CTGPU_OK) return rc;
+  if (bestShape.blocksPerSM == 0)
+    return fail(CTGPU_ERR_UNSUPPORTED, "a problem's tile window is too wide for the batched path");
+  return batch_set_shape(b, bestShape);
+}
+
+extern "C" {
+
+int ctgpu_batch_create(const ctgpu_batch_problem* problems, int n, int flags, ctgpu_batch** out) {
+  if (!problems || !out || n < 1) return fail(CTGPU_ERR_INVALID, "null argument or empty batch");
+  std::unique_ptr<ctgpu_batch> b(new ctgpu_batch);
+  b->flags = flags;
+  b->probs.resize(n);
+  size_t off = 0;
+  for (int i = 0; i < n; i++) {
+    const ctgpu_batch_problem& q = problems[i];
+    BatchEntry& e = b->probs[i];
+    if (!q.d_sino || !q.h_view_angles || !q.d_image)
+      return fail(CTGPU_ERR_INVALID, "problem " + std::to_string(i) + ": null buffer");
+    if (q.geometry.n_view < 1)
+      return fail(CTGPU_ERR_INVALID, "problem " + std::to_string(i) + ": no views");
+    int rc = ctgpu_recon_create(&q.geometry, q.nx, q.ny, q.filter_name, q.filter_param,
+                                q.filter_method, q.zeropad, q.filter_generation, q.interp_name, 1,
+                                q.backproj_name, nullptr, &e.plan);
+    if (rc) return fail(rc, "problem " + std::to_string(i) + ": " + ctgpu_last_error());
+    if (e.plan->bproj == kDiff || e.plan->bproj == kIDiff)
+      return fail(CTGPU_ERR_UNSUPPORTED, "problem " + std::to_string(i) +
+                                             ": diff / idiff backprojectors are not batched");
+    if (q.sino_pitch < q.geometry.n_det) return fail(CTGPU_ERR_INVALID, "sino_pitch < n_det");
+    e.d_sino = q.d_sino;
+    e.sinoPitch = q.sino_pitch;
+    e.d_image = q.d_image;
+    const int nView = q.geometry.n_view;
+    e.filtOff = off;
+    off = align256(off + sizeof(float) * (size_t)nView * e.plan->pitch);
+    e.angOff = off;
+    off = align256(off + sizeof(double) * (size_t)nView);
+    float scale = raw_scale(e.plan);
+    if (e.plan->bproj != kTrig) scale = (float)(scale * e.plan->rotScale);   // PostProcessing
+    // pointers into the arena are filled in below, once it exists
+    e.L = make_launch(e.plan, nView, e.plan->pitch, nullptr, nullptr, e.d_image, 0, scale, 1, 0, 0);
+    if (!table_prep_info(e.L, &e.prep))
+      return fail(CTGPU_ERR_UNSUPPORTED, "problem " + std::to_string(i) +
+                                             ": image pixels behind the fan-beam source");
+    e.scratchOff = off;
+    off = align256(off + e.prep.recBytes + e.prep.rowBytes);
+  }
+  b->arenaBytes = off;
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&b->d_arena), off));
+  for (int i = 0; i < n; i++) {
+    BatchEntry& e = b->probs[i];
+    e.L.angles = reinterpret_cast<const double*>(b->d_arena + e.angOff);
+    e.L.filtered = reinterpret_cast<const float*>(b->d_arena + e.filtOff);
+    CUDA_TRY(cudaMemcpy(b->d_arena + e.angOff, problems[i].h_view_angles,
+                        sizeof(double) * e.L.nViews, cudaMemcpyHostToDevice));
+    const int tiles = ((e.L.nx + 31) / 32) * ((e.L.ny + 31) / 32);
+    for (int t = 0; t < tiles; t++) b->items.push_back(BatchItem{i, t});
+  }
+  // longest first: a tile's cost is its problem's view count
+  std::stable_sort(b->items.begin(), b->items.end(), [&](const BatchItem& x, const BatchItem& y) {
+    return b->probs[x.problem].L.nViews > b->probs[y.problem].L.nViews;
+  });
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&b->d_probs), sizeof(BatchProblem) * n));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&b->d_items), sizeof(BatchItem) * b->items.size()));
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&b->d_counter), sizeof(int)));
+  CUDA_TRY(cudaMemcpy(b->d_items, b->items.data(), sizeof(BatchItem) * b->items.size(),
+                      cudaMemcpyHostToDevice));
+  for (int k = 0; k < kSideStreams; k++) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+  }
+  CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  CUDA_TRY(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking));
+  *out = b.release();
+  return ok();
+}
+
+int ctgpu_batch_run(ctgpu_batch* b, void* stream) {
+  if (!b) return fail(CTGPU_ERR_INVALID, "null batch");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (b->exec) {
+    CUDA_TRY(cudaGraphLaunch(b->exec, s));
+    return ok();
+  }
+  int rc = batch_enqueue_prep(b, s);
+  if (rc) return rc;
+  if (!b->shaped) {
+    rc = (b->flags & CTGPU_BATCH_AUTOTUNE) ? batch_tune(b, s) : batch_set_shape(b, b->shape);
+    if (rc) return rc;
+    b->shaped = true;
+  }
+  rc = batch_enqueue_backprojection(b, s);
+  if (rc) return rc;
+  if (b->flags & CTGPU_BATCH_GRAPH) {
+    // record the same work on a private stream; later runs replay it
+    CUDA_TRY(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal));
+    rc = batch_enqueue_prep(b, b->capture);
+    if (rc == CTGPU_OK) rc = batch_enqueue_backprojection(b, b->capture);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->capture, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    CUDA_TRY(e);
+    b->graph = g;
+    CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  }
+  return ok();
+}
+
+int ctgpu_batch_shape(const ctgpu_batch* b, int* blocksPerSM, int* viewsPerStage) {
+  if (!b) return fail(CTGPU_ERR_INVALID, "null batch");
+  if (blocksPerSM) *blocksPerSM = b->shape.blocksPerSM;
+  if (viewsPerStage) *viewsPerStage = b->shape.cvCap;
+  return ok();
+}
+
+void ctgpu_batch_destroy(ctgpu_batch* b) { delete b; }
 
 }  // extern "C"

@@ -96,6 +96,39 @@ cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int 
                               cudaStream_t s);
 cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
 size_t backproject_scratch_bytes(const BackprojLaunch& L);
+
+// The table-family backprojection as set-up launches plus a main launch, for
+// the batched path (many problems of different sizes, one persistent launch).
+struct TablePrep {
+  int kind;        // main-kernel variant: geometry, interpolation, arctangent
+  int win;         // row elements staged per (tile, view)
+  int rpitch;      // row elements per view
+  int elemBytes;   // bytes per row element (4, 8 or 16)
+  float eps;       // FP32 position margin around jumps of the result
+  size_t recBytes, rowBytes;   // scratch: the records, then the rows
+};
+bool table_prep_info(const BackprojLaunch& L, TablePrep* out);
+// interval rows and (tile, view) records of one problem into scratch
+cudaError_t launch_table_prep(const BackprojLaunch& L, const TablePrep& P, void* scratch,
+                              cudaStream_t s);
+
+struct BatchProblem {
+  BackprojLaunch L;   // one slice: nBatch 1
+  const void* recs;
+  const void* rows;
+  int kind, win, rpitch, elemBytes, cv, tilesX;
+  float eps;
+};
+struct BatchItem { int problem, tile; };
+struct BatchShape { int blocksPerSM, cvCap; };
+// views per pipeline stage of a problem under a launch shape (0: does not fit)
+int batch_views_per_stage(const TablePrep& P, const BatchShape& shape);
+// kernel attributes for a shape; call before capturing a launch in a graph
+cudaError_t prepare_backproject_batch(const BatchShape& shape, int* gridBlocks);
+// d_counter: one int, zero at launch (the work-queue head)
+cudaError_t launch_backproject_batch(const BatchProblem* d_probs, const BatchItem* d_items,
+                                     int nItems, int* d_counter, const BatchShape& shape,
+                                     int gridBlocks, unsigned int* status, cudaStream_t s);
 cudaError_t launch_backproject_views(const BackprojLaunch& L, const void* views, void* scratch,
                                      cudaStream_t s);
 cudaError_t launch_scale_image(float* image, size_t n, float scale, cudaStream_t s);

@@ -170,6 +170,48 @@ class ReconPlan:
             self._h = None
 
 
+class BatchPlan:
+    """Many reconstructions of uneven sizes, one persistent backprojection
+    launch (ctgpu_batch).  `problems`: sequence of dicts with keys geometry,
+    nx, ny, sino (device [n_view, pitch] tensor), angles, image (device
+    [nx, ny] tensor) and optionally filter_name, filter_param, filter_method,
+    zeropad, filter_generation, interp, backproj.  The tensors must outlive
+    the plan; run() reads the sinograms and writes the images."""
+
+    def __init__(self, problems, autotune=True, graph=True):
+        from ._lib import BatchProblem, BATCH_AUTOTUNE, BATCH_GRAPH
+        arr = (BatchProblem * len(problems))()
+        self._keep = []
+        for i, q in enumerate(problems):
+            ang = np.ascontiguousarray(q["angles"], np.float64)
+            names = [enc(q.get(k, d)) for k, d in (("filter_name", "abs_bandlimit"),
+                                                   ("filter_method", "convolution"),
+                                                   ("filter_generation", "direct"),
+                                                   ("interp", "linear"), ("backproj", "table"))]
+            self._keep += [ang] + names + [q["sino"], q["image"]]
+            g = q["geometry"]
+            arr[i] = BatchProblem(g, q["nx"], q["ny"], names[0], float(q.get("filter_param", -1.0)),
+                                  names[1], int(q.get("zeropad", 1)), names[2], names[3], names[4],
+                                  q["sino"].data_ptr(), q["sino"].shape[1],
+                                  ang.ctypes.data, q["image"].data_ptr())
+        self._h = C.c_void_p()
+        flags = (BATCH_AUTOTUNE if autotune else 0) | (BATCH_GRAPH if graph else 0)
+        check(lib().ctgpu_batch_create(arr, len(problems), flags, C.byref(self._h)))
+
+    def run(self, stream=None):
+        check(lib().ctgpu_batch_run(self._h, stream_handle(stream)))
+
+    def shape(self):
+        a, b = C.c_int(), C.c_int()
+        check(lib().ctgpu_batch_shape(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().ctgpu_batch_destroy(self._h)
+            self._h = None
+
+
 def helical180li(geometry, sino, interp_view=-1, stream=None):
     """Projections::Helical180LI on a device sinogram; returns (out, angles)."""
     torch = _torch()

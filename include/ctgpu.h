@@ -197,6 +197,44 @@ int ctgpu_recon_project(ctgpu_recon* r, const float* d_image, const double* h_vi
 void ctgpu_recon_destroy(ctgpu_recon* r);
 
 /* ------------------------------------------------------------------------ */
+/* Batched reconstruction of many problems of uneven sizes.  No reference   */
+/* counterpart as one call: it is the reference's Reconstructor +           */
+/* reconstructAllViews (reconstruct.cpp:50-239) for each problem, with the  */
+/* problems' backprojections sharing one persistent launch.                 */
+/* ------------------------------------------------------------------------ */
+typedef struct ctgpu_batch ctgpu_batch;
+typedef struct {
+  ctgpu_geometry geometry;          /* the problem's scan (.pj header fields) */
+  int nx, ny;                       /* image size */
+  const char* filter_name;          /* as ctgpu_recon_create */
+  double filter_param;
+  const char* filter_method;
+  int zeropad;
+  const char* filter_generation;
+  const char* interp_name;          /* nearest, linear, cubic */
+  const char* backproj_name;        /* table or trig (parallel); fan beams use their own */
+  const float* d_sino;              /* device [n_view][sino_pitch], read at every run */
+  int sino_pitch;
+  const double* h_view_angles;      /* n_view angles, copied at create */
+  float* d_image;                   /* device [nx][ny], written at every run */
+} ctgpu_batch_problem;
+#define CTGPU_BATCH_AUTOTUNE 1   /* time the launch shapes on the first run, keep the fastest */
+#define CTGPU_BATCH_GRAPH 2      /* capture the batch in a CUDA graph after the first run, replay it */
+/* Plans every problem (filters, windows, work list); diff / idiff are not
+ * batched (CTGPU_ERR_UNSUPPORTED).  The buffers named by the problems must
+ * stay valid while the batch is used. */
+int ctgpu_batch_create(const ctgpu_batch_problem* problems, int n_problems, int flags,
+                       ctgpu_batch** out);
+/* Filters and backprojects every problem (PostProcessing included) on
+ * `stream`; stream-ordered, so check with ctgpu_sync.  The first run sets the
+ * launch shape (tuned when CTGPU_BATCH_AUTOTUNE) and, with CTGPU_BATCH_GRAPH,
+ * captures later runs' work as one CUDA graph. */
+int ctgpu_batch_run(ctgpu_batch* b, void* stream);
+/* the launch shape in use: resident blocks per SM and views per pipeline stage cap */
+int ctgpu_batch_shape(const ctgpu_batch* b, int* blocks_per_sm, int* views_per_stage);
+void ctgpu_batch_destroy(ctgpu_batch* b);
+
+/* ------------------------------------------------------------------------ */
 /* Helical -- replaces Projections::Helical180LI / Helical180LI_Equiangular */
 /* and HalfScanFeather (libctsim/projections.cpp:200-439)                     */
 /* ------------------------------------------------------------------------ */
