@@ -230,9 +230,14 @@ struct ctgpu_scanner {
   size_t d_views_cap = 0;
   float* d_sino = nullptr;
   size_t d_sino_cap = 0;
+  // collect_projections_batch: the phantoms' elements back to back, offsets
+  PElem* d_belems = nullptr;
+  size_t d_belems_cap = 0;
+  int* d_boffs = nullptr;
+  size_t d_boffs_cap = 0;
   ~ctgpu_scanner() {
-    if (d_views) cudaFree(d_views);
-    if (d_sino) cudaFree(d_sino);
+    for (void* p : {(void*)d_views, (void*)d_sino, (void*)d_belems, (void*)d_boffs})
+      if (p) cudaFree(p);
   }
 };
 
@@ -551,6 +556,64 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "too many phantom elements x rays per detector for one CTA");
   CUDA_TRY(e);
+  return ok();
+}
+
+int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const* phantoms,
+                                    int n, float* d_sinos, int pitch, long long sliceStride,
+                                    double* h_angles, void* stream) {
+  if (!s || !phantoms || !d_sinos || n < 1) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (pitch < s->nDet) return fail(CTGPU_ERR_INVALID, "sinogram pitch smaller than nDet");
+  if (sliceStride < (long long)pitch * s->nView) return fail(CTGPU_ERR_INVALID, "slice stride too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<PElem> all;
+  std::vector<int> offs(1, 0);
+  int maxElem = 0;
+  for (int z = 0; z < n; z++) {
+    const ctgpu_phantom* p = phantoms[z];
+    if (!p) return fail(CTGPU_ERR_INVALID, "null phantom");
+    if (p->unitPulse) return fail(CTGPU_ERR_UNSUPPORTED, "unit-pulse phantoms are not batched");
+    all.insert(all.end(), p->elems.begin(), p->elems.end());
+    offs.push_back((int)all.size());
+    maxElem = std::max(maxElem, (int)p->elems.size());
+  }
+  scanner_views(s, 0, s->nView, 0);
+  if (h_angles)
+    for (int v = 0; v < s->nView; v++) h_angles[v] = s->views[v].angle;
+  CUDA_TRY(ensure_device(s->d_belems, s->d_belems_cap, all.size()));
+  CUDA_TRY(ensure_device(s->d_boffs, s->d_boffs_cap, offs.size()));
+  CUDA_TRY(ensure_device(s->d_views, s->d_views_cap, (size_t)s->nView));
+  if (!all.empty())
+    CUDA_TRY(cudaMemcpyAsync(s->d_belems, all.data(), sizeof(PElem) * all.size(),
+                             cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(s->d_boffs, offs.data(), sizeof(int) * offs.size(),
+                           cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(s->d_views, s->views.data(), sizeof(ViewPos) * s->nView,
+                           cudaMemcpyHostToDevice, st));
+  RaysumLaunch L{};
+  L.geometry = s->geometry;
+  L.nDet = s->nDet;
+  L.nSample = s->nSample;
+  L.nElem = maxElem;
+  L.nViews = s->nView;
+  L.pitch = pitch;
+  L.rowOffset = 0;
+  L.centerDetectorLength = s->centerDetectorLength;
+  L.angularDetLen = s->angularDetLen;
+  L.angularDetInc = s->angularDetInc;
+  L.elems = s->d_belems;
+  L.views = s->d_views;
+  L.sino = d_sinos;
+  L.status = status_pointer();
+  L.nSlices = n;
+  L.elemOffset = s->d_boffs;
+  L.sliceStride = (size_t)sliceStride;
+  cudaError_t e = launch_raysum(L, st);
+  if (e == cudaErrorInvalidValue)
+    return fail(CTGPU_ERR_UNSUPPORTED, "too many phantom elements x rays per detector for one CTA");
+  CUDA_TRY(e);
+  // (copies from pageable host memory are staged before cudaMemcpyAsync
+  // returns, so the vectors may go)
   return ok();
 }
 

@@ -39,6 +39,12 @@ struct RaysumLaunch {
   const ViewPos* views;
   float* sino;
   unsigned int* status;
+  // several phantoms, one sinogram each (grid.y): phantom z's elements are
+  // elems[elemOffset[z] .. elemOffset[z+1]); nElem is then the largest count.
+  // elemOffset null: one phantom of nElem elements.
+  int nSlices;
+  const int* elemOffset;
+  size_t sliceStride;   // floats between the sinograms
 };
 
 // Filter: out[v][n] = sum_i (w[i] * in[v][i]) * taps[n - i + nDet - 1]

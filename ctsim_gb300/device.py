@@ -52,6 +52,22 @@ def raysums(scanner, phantom, sino, start_view=0, n_views=None, offset_view=None
     return ang
 
 
+def raysums_batch(scanner, phantoms, sinos, stream=None):
+    """collectProjections of every phantom with one scanner, one launch:
+    sinos [B, n_view, pitch] device tensor; returns the view angles."""
+    g = scanner.geometry()
+    if sinos.shape[0] != len(phantoms) or sinos.shape[1] < g.n_view or not sinos.is_contiguous():
+        raise ValueError("sinos must be a contiguous [B, n_view, pitch] tensor")
+    hs = (C.c_void_p * len(phantoms))(*[p._h.value if hasattr(p._h, "value") else p._h
+                                        for p in phantoms])
+    ang = np.zeros(g.n_view, np.float64)
+    check(lib().ctgpu_collect_projections_batch(scanner._h, hs, len(phantoms), _ptr(sinos),
+                                                sinos.shape[2], sinos.stride(0),
+                                                ang.ctypes.data_as(C.c_void_p),
+                                                stream_handle(stream)))
+    return ang
+
+
 class ReconPlan:
     """A Reconstructor for device tensors (ctgpu_recon)."""
 

@@ -118,6 +118,14 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
 int ctgpu_collect_projections_host(ctgpu_scanner* s, const ctgpu_phantom* p, int start_view,
                                    int n_views, int offset_view, int storage_offset,
                                    float* h_sino, double* h_view_angles);
+/* collectProjections of all n_view views for n_phantoms phantoms at once (one
+ * launch): sinogram z at d_sinos + z * sino_slice_stride floats.  No
+ * reference counterpart as one call (the reference scans one phantom per
+ * Scanner::collectProjections).  Unit-pulse phantoms are not batched. */
+int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const* phantoms,
+                                    int n_phantoms, float* d_sinos, int sino_pitch,
+                                    long long sino_slice_stride, double* h_view_angles,
+                                    void* stream);
 void ctgpu_scanner_destroy(ctgpu_scanner* s);
 
 /* ------------------------------------------------------------------------ */

@@ -288,3 +288,24 @@ def test_batch_host_equals_device_batch(gpu, pinned):
     r = ref.cpu().numpy()
     for b in range(B):
         assert rel_l2(res[b], r[b]) < 1e-7, b
+
+
+@pytest.mark.parametrize("geo,nray", [("parallel", 2), ("equiangular", 1), ("equilinear", 3)])
+def test_raysums_batch_equals_single(gpu, geo, nray):
+    """ctgpu_collect_projections_batch (all phantoms in one launch) writes the
+    same sinogram bits as one collectProjections per phantom."""
+    torch, cg, device = gpu
+    from ctsim_gb300 import phantoms as P
+    phs = [cg.Phantom("herman"), cg.Phantom("shepp-logan")] + \
+          [P.make_phantom(P.random_ellipses(seed=70 + i, n=3 + 4 * i)) for i in range(4)]
+    sc = cg.Scanner(phs[0], geo, 157, 96, nSample=nray)
+    g = sc.geometry()
+    pitch = device.pitch_for(157)
+    batch = torch.zeros((len(phs), 96, pitch), device="cuda")
+    ang_b = device.raysums_batch(sc, phs, batch)
+    for i, ph in enumerate(phs):
+        one = device.alloc_sinogram(96, 157)
+        ang = device.raysums(sc, ph, one)
+        cg.sync()
+        assert np.array_equal(ang, ang_b)
+        assert torch.equal(one[:, :157], batch[i, :, :157]), i
