@@ -164,6 +164,15 @@ PElem make_elem(int type, double cx, double cy, double u, double v, double rotDe
     e.bx0 = std::fmin(e.bx0, x[i]); e.bx1 = std::fmax(e.bx1, x[i]);
     e.by0 = std::fmin(e.by0, y[i]); e.by1 = std::fmax(e.by1, y[i]);
   }
+  const double hx = 0.5 * (e.bx1 - e.bx0), hy = 0.5 * (e.by1 - e.by0);
+  e.dcbx = (float)(0.5 * (e.bx0 + e.bx1) - cx);
+  e.dcby = (float)(0.5 * (e.by0 + e.by1) - cy);
+  e.hx = (float)hx;
+  e.hy = (float)hy;
+  e.rbox = (float)(std::sqrt(hx * hx + hy * hy) * (1.0 + 1e-5) + 1e-7);
+  // a line this close to the box centre crosses the box for certain: the
+  // kernel's FP32 box test margin (1e-5 (hx + hy)) and its rounding stay inside
+  e.rin = (float)(std::fmin(hx, hy) - 2e-5 * (hx + hy) - 1e-7);
   return e;
 }
 

@@ -24,6 +24,10 @@ struct PElem {
   double cx, cy, u, v, rot, atten;
   double cosr, sinr;
   double bx0, by0, bx1, by1;   // outline-polygon bounding box
+  // view-independent FP32 values of the ray-sum kernel, set with the box:
+  // box centre minus element centre, box half sizes, circumscribed radius
+  // (widened by its margin), inscribed radius less the margin
+  float dcbx, dcby, hx, hy, rbox, rin;
 };
 
 // Source / detector end points of one view after the reference's incremental

@@ -221,25 +221,28 @@ __device__ __forceinline__ void split_root(double t, int& ti, float& tf) {
   tf = (float)(t - fl);
 }
 
+// Per-view FP64 quantities of the equiangular set-up shared by all elements:
+// unit vectors of the first ray's arc angle alpha0 and of the arc's middle,
+// and mid - alpha0.
+struct ArcFrame {
+  double c0, s0, cm, sm, midRel, invDelta;
+};
+
 template <int GEOM>
-__device__ void setup_element(const RaysumLaunch& L, const ViewGeom& g, const PElem& pe, int sub,
-                              ElemView& e) {
+__device__ void setup_element(const RaysumLaunch& L, const ViewGeom& g, const ArcFrame& af,
+                              const PElem& pe, int sub, ElemView& e) {
   e.type = pe.type;
   e.ca = (float)pe.cosr;
   e.sa = (float)pe.sinr;
   e.u = (float)pe.u;
   e.v = (float)pe.v;
   e.atten = (float)pe.atten;
-  double cbx = 0.5 * (pe.bx0 + pe.bx1), cby = 0.5 * (pe.by0 + pe.by1);
-  double hx = 0.5 * (pe.bx1 - pe.bx0), hy = 0.5 * (pe.by1 - pe.by0);
-  e.dcbx = (float)(cbx - pe.cx);
-  e.dcby = (float)(cby - pe.cy);
-  e.hx = (float)hx;
-  e.hy = (float)hy;
-  e.rbox = (float)(sqrt(hx * hx + hy * hy) * (1.0 + 1e-5) + 1e-7);
-  // a line this close to the box centre crosses the box for certain: the
-  // FP32 test's margin (1e-5 (hx + hy)) and its rounding stay inside
-  e.rin = (float)(fmin(hx, hy) - 2e-5 * (hx + hy) - 1e-7);
+  e.dcbx = pe.dcbx;
+  e.dcby = pe.dcby;
+  e.hx = pe.hx;
+  e.hy = pe.hy;
+  e.rbox = pe.rbox;
+  e.rin = pe.rin;
   e.live = 1;
   e.cpsi = e.spsi = 0.f;
   e.ra = e.rb = 0.f;
@@ -265,46 +268,52 @@ __device__ void setup_element(const RaysumLaunch& L, const ViewGeom& g, const PE
     split_root(-A / B, e.tcI, e.tcF);
     e.kB = (float)B;
   } else {
-    double CD = L.centerDetectorLength;
-    double wx = pe.cx - g.S0x, wy = pe.cy - g.S0y;
-    double wn = sqrt(wx * wx + wy * wy);
-    double thw = atan2(wy, wx);
-    double K = cross2(g.S0x, g.S0y, wx, wy);
-    double q = K / (CD * wn);
+    // The arc point D(a) = CD (cos a, sin a) sees the element centre W from the
+    // source S when cross(D(a) - S, W - S) = 0, i.e. sin(theta_w - a) = q with
+    // w = W - S, theta_w its angle and q = cross(S, w) / (CD |w|).  The two
+    // solutions a = theta_w - b and theta_w - pi + b (sin b = q) have the unit
+    // vectors R(-b) w/|w| and -R(b) w/|w|; the one nearer the arc's middle is
+    // taken, and its angle is measured from the middle (atan2 in (-pi, pi]),
+    // which is the reference's branch choice without an arcsine.
+    const double CD = L.centerDetectorLength;
+    const double wx = pe.cx - g.S0x, wy = pe.cy - g.S0y;
+    const double wn = sqrt(wx * wx + wy * wy);
+    const double q = cross2(g.S0x, g.S0y, wx, wy) / (CD * wn);
     if (!(fabs(q) <= 1.0)) { e.live = 0; return; }
-    double as = asin(q);
-    // the two arc angles whose ray passes through the element centre; take the
-    // one nearest the middle of this view's detector arc
-    double mid = g.alpha0 + 0.5 * (L.nDet * L.nSample - 1) * g.delta;
-    double best = 0, bestd = 1e300;
-    for (int c = 0; c < 2; c++) {
-      double a = (c == 0) ? thw - as : thw - kPi + as;
-      double k = floor((mid - a) / kTwoPi + 0.5);
-      a += k * kTwoPi;
-      double d = fabs(a - mid);
-      if (d < bestd) { bestd = d; best = a; }
-    }
-    double tc = (best - g.alpha0) / g.delta;
-    split_root(tc, e.tcI, e.tcF);
+    const double cb = sqrt((1.0 - q) * (1.0 + q));
+    const double iw = 1.0 / wn;
+    const double u1x = (wx * cb + wy * q) * iw, u1y = (wy * cb - wx * q) * iw;
+    const double u2x = -(wx * cb - wy * q) * iw, u2y = -(wy * cb + wx * q) * iw;
+    const double d1 = u1x * af.cm + u1y * af.sm, d2 = u2x * af.cm + u2y * af.sm;
+    const double ux = d1 >= d2 ? u1x : u2x, uy = d1 >= d2 ? u1y : u2y;
+    const double rel = atan2(af.cm * uy - af.sm * ux, af.cm * ux + af.sm * uy) + af.midRel;
+    split_root(rel * af.invDelta, e.tcI, e.tcF);
     e.kB = (float)(2.0 * CD * wn);
-    double psi = thw - 0.5 * best - 0.5 * g.alpha0;
-    psi -= kTwoPi * floor(psi / kTwoPi);
-    double sp, cp;
-    sincos(psi, &sp, &cp);
-    e.cpsi = (float)cp;
-    e.spsi = (float)sp;
+    // psi = theta_w - (a + alpha0)/2 = (theta_w - alpha0) - rel/2 enters only
+    // through its cosine and sine: FP32
+    const float thw0 = atan2f((float)(af.c0 * wy - af.s0 * wx), (float)(af.c0 * wx + af.s0 * wy));
+    float sp, cp;
+    sincosf(thw0 - 0.5f * (float)rel, &sp, &cp);
+    e.cpsi = cp;
+    e.spsi = sp;
   }
 }
 
 }  // namespace
 
+// per-view values, computed once per CTA by one thread (FP64 is 1/64 of the
+// FP32 rate on this GPU)
+struct ViewShared {
+  ViewGeom g;
+  ArcFrame af;
+  double ca0, sa0;
+};
+
 template <int GEOM>
 __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
   extern __shared__ __align__(16) ElemView ev[];
+  __shared__ ViewShared vs;
   const int view = blockIdx.x;
-  const ViewPos vp = L.views[view];
-  ViewGeom g;
-  view_geom<GEOM>(L, vp, g);
   const int nS = L.nSample;
   const int nSub = (GEOM == kParallel) ? nS : 1;
   const PElem* elems = L.elems;
@@ -314,10 +323,28 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
     elems += L.elemOffset[blockIdx.y];
     nElem = L.elemOffset[blockIdx.y + 1] - L.elemOffset[blockIdx.y];
   }
+  if (threadIdx.x == 0) {
+    const ViewPos vp = L.views[view];
+    view_geom<GEOM>(L, vp, vs.g);
+    vs.af = ArcFrame{};
+    vs.ca0 = 1.0;
+    vs.sa0 = 0.0;
+    if (GEOM == kEquiangular) {
+      const double mid = vs.g.alpha0 + 0.5 * (L.nDet * L.nSample - 1) * vs.g.delta;
+      sincos(vs.g.alpha0, &vs.af.s0, &vs.af.c0);
+      sincos(mid, &vs.af.sm, &vs.af.cm);
+      vs.af.midRel = mid - vs.g.alpha0;
+      vs.af.invDelta = 1.0 / vs.g.delta;
+      vs.ca0 = vs.af.c0;
+      vs.sa0 = vs.af.s0;
+    }
+  }
+  __syncthreads();
+  const ViewGeom& g = vs.g;
   float2* sdir = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(ev) +
                                            dir_table_offset(L.nElem * nSub));   // per sub-sample
   for (int k = threadIdx.x; k < nElem * nSub; k += blockDim.x)
-    setup_element<GEOM>(L, g, elems[k / nSub], k % nSub, ev[k]);
+    setup_element<GEOM>(L, g, vs.af, elems[k / nSub], k % nSub, ev[k]);
   if (GEOM == kParallel) {
     for (int i = threadIdx.x; i < nS; i += blockDim.x) {
       double drx = (g.D0x + i * g.dDx) - g.S0x, dry = (g.D0y + i * g.dDy) - g.S0y;
@@ -331,10 +358,7 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
   const float rsx = (float)(g.D0x - g.S0x), rsy = (float)(g.D0y - g.S0y);
   const float stx = (float)g.dDx, sty = (float)g.dDy;
   const float hdelta = (float)(0.5 * g.delta);
-  double ca0, sa0;
-  if (GEOM == kEquiangular) sincos(g.alpha0, &sa0, &ca0);
-  else { ca0 = 1; sa0 = 0; }
-  const float fca0 = (float)ca0, fsa0 = (float)sa0;
+  const float fca0 = (float)vs.ca0, fsa0 = (float)vs.sa0;
   const float CD = (float)L.centerDetectorLength;
   const float Sx = (float)g.S0x, Sy = (float)g.S0y;
 

@@ -62,6 +62,8 @@ def test_raysums_match_reference(gpu, golden, name):
     np.testing.assert_array_equal(ang, d[name + "/angles"])
     out = sino[:, :g.n_det].cpu().numpy()
     ref = d[name + "/data"]
+    print("raysums %s: rel-L2 %.3g, max |err| / max %.3g" % (
+        name, rel_l2(out, ref), np.abs(out - ref).max() / max(np.abs(ref).max(), 1e-30)))
     assert rel_l2(out, ref) < TOL, rel_l2(out, ref)
     assert np.abs(out - ref).max() <= 1e-4 * max(np.abs(ref).max(), 1e-30)
 
