@@ -235,8 +235,12 @@ struct ctgpu_scanner {
   double xs1, ys1, xs2, ys2, xd1 = 0, yd1 = 0, xd2 = 0, yd2 = 0;
   M3 inc;
   std::vector<ViewPos> views;
-  ViewPos* d_views = nullptr;
+  RayView* d_views = nullptr;
   size_t d_views_cap = 0;
+  float2* d_sdirs = nullptr;
+  size_t d_sdirs_cap = 0;
+  unsigned char* d_records = nullptr;
+  size_t d_records_cap = 0;
   float* d_sino = nullptr;
   size_t d_sino_cap = 0;
   // collect_projections_batch: the phantoms' elements back to back, offsets
@@ -245,7 +249,8 @@ struct ctgpu_scanner {
   int* d_boffs = nullptr;
   size_t d_boffs_cap = 0;
   ~ctgpu_scanner() {
-    for (void* p : {(void*)d_views, (void*)d_sino, (void*)d_belems, (void*)d_boffs})
+    for (void* p : {(void*)d_views, (void*)d_sino, (void*)d_belems, (void*)d_boffs,
+                    (void*)d_sdirs, (void*)d_records})
       if (p) cudaFree(p);
   }
 };
@@ -527,6 +532,76 @@ static void scanner_views(ctgpu_scanner* s, int startView, int nViews, int offse
   }
 }
 
+}  // extern "C"
+
+// Scanner::projectSingleView's per-view ray geometry (scanner.cpp:445-533)
+// in FP64, once per view for every phantom.
+RayView ctgpu::make_ray_view(int geometry, int nDet, int nS, double angularDetLen,
+                             double angularDetInc, const ViewPos& vp) {
+  RayView g{};
+  const double sdx = (vp.xs2 - vp.xs1) / nDet, sdy = (vp.ys2 - vp.ys1) / nDet;
+  g.S0x = vp.xs1 + sdx / 2;
+  g.S0y = vp.ys1 + sdy / 2;
+  g.dSx = sdx;
+  g.dSy = sdy;
+  g.c0 = 1.0;
+  if (geometry == kEquiangular) {
+    g.delta = angularDetInc / nS;
+    g.alpha0 = vp.angle + 3 * kHalfPi - (angularDetLen / 2) + g.delta / 2;
+    const double mid = g.alpha0 + 0.5 * (nDet * nS - 1) * g.delta;
+    g.c0 = std::cos(g.alpha0);
+    g.s0 = std::sin(g.alpha0);
+    g.cm = std::cos(mid);
+    g.sm = std::sin(mid);
+    g.midRel = mid - g.alpha0;
+    g.invDelta = 1.0 / g.delta;
+  } else {
+    const double ddx = (vp.xd2 - vp.xd1) / nDet, ddy = (vp.yd2 - vp.yd1) / nDet;
+    const double ddx2 = ddx / nS, ddy2 = ddy / nS;
+    g.D0x = vp.xd1 + ddx2 / 2;
+    g.D0y = vp.yd1 + ddy2 / 2;
+    g.dDx = ddx2;
+    g.dDy = ddy2;
+  }
+  g.rsx = (float)(g.D0x - g.S0x);
+  g.rsy = (float)(g.D0y - g.S0y);
+  g.stx = (float)g.dDx;
+  g.sty = (float)g.dDy;
+  g.hdelta = (float)(0.5 * g.delta);
+  g.ca0 = (float)g.c0;
+  g.sa0 = (float)g.s0;
+  g.Sx = (float)g.S0x;
+  g.Sy = (float)g.S0y;
+  return g;
+}
+
+// the scanner's current views as ray records (+ parallel ray directions) on the device
+static cudaError_t upload_ray_views(ctgpu_scanner* s, int nViews, cudaStream_t st) {
+  std::vector<RayView> rv(nViews);
+  for (int v = 0; v < nViews; v++)
+    rv[v] = make_ray_view(s->geometry, s->nDet, s->nSample, s->angularDetLen, s->angularDetInc,
+                          s->views[v]);
+  cudaError_t e = ensure_device(s->d_views, s->d_views_cap, (size_t)nViews);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->d_views, rv.data(), sizeof(RayView) * nViews, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess || s->geometry != kParallel) return e;
+  std::vector<float2> dirs((size_t)nViews * s->nSample);
+  for (int v = 0; v < nViews; v++)
+    for (int i = 0; i < s->nSample; i++) {
+      const RayView& g = rv[v];
+      double drx = (g.D0x + i * g.dDx) - g.S0x, dry = (g.D0y + i * g.dDy) - g.S0y;
+      double inv = 1.0 / std::sqrt(drx * drx + dry * dry);
+      dirs[(size_t)v * s->nSample + i] = make_float2((float)(drx * inv), (float)(dry * inv));
+    }
+  e = ensure_device(s->d_sdirs, s->d_sdirs_cap, dirs.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->d_sdirs, dirs.data(), sizeof(float2) * dirs.size(),
+                        cudaMemcpyHostToDevice, st);
+  return e;
+}
+
+extern "C" {
+
 int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int startView,
                               int nViews, int offsetView, int storageOffset, float* d_sino,
                               int pitch, double* h_angles, void* stream) {
@@ -543,9 +618,7 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
     return ok();
   }
   CUDA_TRY(const_cast<ctgpu_phantom*>(p)->upload(st));
-  CUDA_TRY(ensure_device(s->d_views, s->d_views_cap, (size_t)nViews));
-  CUDA_TRY(cudaMemcpyAsync(s->d_views, s->views.data(), sizeof(ViewPos) * nViews,
-                           cudaMemcpyHostToDevice, st));
+  CUDA_TRY(upload_ray_views(s, nViews, st));
   RaysumLaunch L{};
   L.geometry = s->geometry;
   L.nDet = s->nDet;
@@ -559,8 +632,11 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
   L.angularDetInc = s->angularDetInc;
   L.elems = p->d_elems;
   L.views = s->d_views;
+  L.sdirs = s->d_sdirs;
   L.sino = d_sino;
   L.status = status_pointer();
+  CUDA_TRY(ensure_device(s->d_records, s->d_records_cap, raysum_record_bytes(L, L.nElem)));
+  L.records = s->d_records;
   cudaError_t e = launch_raysum(L, st);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "too many phantom elements x rays per detector for one CTA");
@@ -591,13 +667,11 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
     for (int v = 0; v < s->nView; v++) h_angles[v] = s->views[v].angle;
   CUDA_TRY(ensure_device(s->d_belems, s->d_belems_cap, all.size()));
   CUDA_TRY(ensure_device(s->d_boffs, s->d_boffs_cap, offs.size()));
-  CUDA_TRY(ensure_device(s->d_views, s->d_views_cap, (size_t)s->nView));
+  CUDA_TRY(upload_ray_views(s, s->nView, st));
   if (!all.empty())
     CUDA_TRY(cudaMemcpyAsync(s->d_belems, all.data(), sizeof(PElem) * all.size(),
                              cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(s->d_boffs, offs.data(), sizeof(int) * offs.size(),
-                           cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(s->d_views, s->views.data(), sizeof(ViewPos) * s->nView,
                            cudaMemcpyHostToDevice, st));
   RaysumLaunch L{};
   L.geometry = s->geometry;
@@ -612,11 +686,14 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   L.angularDetInc = s->angularDetInc;
   L.elems = s->d_belems;
   L.views = s->d_views;
+  L.sdirs = s->d_sdirs;
   L.sino = d_sinos;
   L.status = status_pointer();
   L.nSlices = n;
   L.elemOffset = s->d_boffs;
   L.sliceStride = (size_t)sliceStride;
+  CUDA_TRY(ensure_device(s->d_records, s->d_records_cap, raysum_record_bytes(L, (int)all.size())));
+  L.records = s->d_records;
   cudaError_t e = launch_raysum(L, st);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "too many phantom elements x rays per detector for one CTA");

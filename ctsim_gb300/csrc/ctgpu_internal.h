@@ -36,11 +36,28 @@ struct ViewPos {
   double xs1, ys1, xs2, ys2, xd1, yd1, xd2, yd2, angle;
 };
 
+// Per-view ray geometry derived on the host in FP64 from a ViewPos (shared by
+// every phantom scanned with the view), with the FP32 copies the rays use.
+struct RayView {
+  double S0x, S0y, dSx, dSy;       // source of detector 0 (parallel: per detector step)
+  double D0x, D0y, dDx, dDy;       // detector point of ray 0 and per-ray step
+  double alpha0, delta;            // equiangular arc: angle of ray 0, step
+  double c0, s0, cm, sm;           // equiangular: cos/sin of alpha0 and of the arc's middle
+  double midRel, invDelta;         // middle - alpha0, 1 / delta
+  float rsx, rsy, stx, sty;        // FP32: D0 - S0, per-ray step
+  float hdelta, ca0, sa0, Sx, Sy;  // FP32: delta / 2, cos/sin alpha0, source
+  float pad[3];
+};
+RayView make_ray_view(int geometry, int nDet, int nSample, double angularDetLen,
+                      double angularDetInc, const ViewPos& vp);
+
 struct RaysumLaunch {
   int geometry, nDet, nSample, nElem, nViews, pitch, rowOffset;
   double centerDetectorLength, angularDetLen, angularDetInc;
   const PElem* elems;
-  const ViewPos* views;
+  const RayView* views;   // nViews
+  const float2* sdirs;    // parallel: [nViews][nSample] unit ray directions
+  void* records;          // scratch: raysum_record_bytes()
   float* sino;
   unsigned int* status;
   // several phantoms, one sinogram each (grid.y): phantom z's elements are
@@ -102,6 +119,8 @@ cudaError_t status_read_and_clear(unsigned int* value);
 
 // kernel entry wrappers (defined in the .cu files)
 cudaError_t launch_raysum(const RaysumLaunch& L, cudaStream_t s);
+// scratch of launch_raysum: one record per (phantom, view, element, ray sample)
+size_t raysum_record_bytes(const RaysumLaunch& L, int totalElems);
 cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int rowOffset,
                               cudaStream_t s);
 cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);

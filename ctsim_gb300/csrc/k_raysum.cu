@@ -183,36 +183,6 @@ __device__ __forceinline__ int box_test(const ElemView& e, float rho, float rx, 
   return 1;
 }
 
-struct ViewGeom {   // FP64 per-view quantities shared by the setup and the rays
-  double S0x, S0y, dSx, dSy;       // source (parallel: per detector step)
-  double D0x, D0y, dDx, dDy;       // detector point of ray 0 and per-ray step
-  double dDetx, dDety;             // parallel: per-detector detector step
-  double alpha0, delta;            // equiangular arc: angle of ray 0, step
-};
-
-template <int GEOM>
-__device__ void view_geom(const RaysumLaunch& L, const ViewPos& vp, ViewGeom& g) {
-  int nDet = L.nDet, nS = L.nSample;
-  double sdx = (vp.xs2 - vp.xs1) / nDet, sdy = (vp.ys2 - vp.ys1) / nDet;
-  g.S0x = vp.xs1 + sdx / 2;
-  g.S0y = vp.ys1 + sdy / 2;
-  g.dSx = sdx;
-  g.dSy = sdy;
-  if (GEOM == kEquiangular) {
-    g.delta = L.angularDetInc / nS;
-    g.alpha0 = vp.angle + 3 * kHalfPi - (L.angularDetLen / 2) + g.delta / 2;
-  } else {
-    double ddx = (vp.xd2 - vp.xd1) / nDet, ddy = (vp.yd2 - vp.yd1) / nDet;
-    double ddx2 = ddx / nS, ddy2 = ddy / nS;
-    g.D0x = vp.xd1 + ddx2 / 2;
-    g.D0y = vp.yd1 + ddy2 / 2;
-    g.dDx = ddx2;
-    g.dDy = ddy2;
-    g.dDetx = ddx;
-    g.dDety = ddy;
-  }
-}
-
 __device__ __forceinline__ void split_root(double t, int& ti, float& tf) {
   double fl = floor(t);
   if (fl > 2.0e9) fl = 2.0e9;
@@ -221,15 +191,9 @@ __device__ __forceinline__ void split_root(double t, int& ti, float& tf) {
   tf = (float)(t - fl);
 }
 
-// Per-view FP64 quantities of the equiangular set-up shared by all elements:
-// unit vectors of the first ray's arc angle alpha0 and of the arc's middle,
-// and mid - alpha0.
-struct ArcFrame {
-  double c0, s0, cm, sm, midRel, invDelta;
-};
-
+// FP64 set-up of one (view, element[, ray sample]) record.
 template <int GEOM>
-__device__ void setup_element(const RaysumLaunch& L, const ViewGeom& g, const ArcFrame& af,
+__device__ void setup_element(const RaysumLaunch& L, const RayView& g, const float2* sdir,
                               const PElem& pe, int sub, ElemView& e) {
   e.type = pe.type;
   e.ca = (float)pe.cosr;
@@ -246,6 +210,9 @@ __device__ void setup_element(const RaysumLaunch& L, const ViewGeom& g, const Ar
   e.live = 1;
   e.cpsi = e.spsi = 0.f;
   e.ra = e.rb = 0.f;
+  e.kB = 0.f;
+  e.tcI = 0;
+  e.tcF = 0.f;
   if (GEOM == kParallel) {
     // ray direction of sub-sample `sub` (independent of the detector index)
     double rx = (g.D0x + sub * g.dDx) - g.S0x, ry = (g.D0y + sub * g.dDy) - g.S0y;
@@ -284,14 +251,14 @@ __device__ void setup_element(const RaysumLaunch& L, const ViewGeom& g, const Ar
     const double iw = 1.0 / wn;
     const double u1x = (wx * cb + wy * q) * iw, u1y = (wy * cb - wx * q) * iw;
     const double u2x = -(wx * cb - wy * q) * iw, u2y = -(wy * cb + wx * q) * iw;
-    const double d1 = u1x * af.cm + u1y * af.sm, d2 = u2x * af.cm + u2y * af.sm;
+    const double d1 = u1x * g.cm + u1y * g.sm, d2 = u2x * g.cm + u2y * g.sm;
     const double ux = d1 >= d2 ? u1x : u2x, uy = d1 >= d2 ? u1y : u2y;
-    const double rel = atan2(af.cm * uy - af.sm * ux, af.cm * ux + af.sm * uy) + af.midRel;
-    split_root(rel * af.invDelta, e.tcI, e.tcF);
+    const double rel = atan2(g.cm * uy - g.sm * ux, g.cm * ux + g.sm * uy) + g.midRel;
+    split_root(rel * g.invDelta, e.tcI, e.tcF);
     e.kB = (float)(2.0 * CD * wn);
     // psi = theta_w - (a + alpha0)/2 = (theta_w - alpha0) - rel/2 enters only
     // through its cosine and sine: FP32
-    const float thw0 = atan2f((float)(af.c0 * wy - af.s0 * wx), (float)(af.c0 * wx + af.s0 * wy));
+    const float thw0 = atan2f((float)(g.c0 * wy - g.s0 * wx), (float)(g.c0 * wx + g.s0 * wy));
     float sp, cp;
     sincosf(thw0 - 0.5f * (float)rel, &sp, &cp);
     e.cpsi = cp;
@@ -301,66 +268,60 @@ __device__ void setup_element(const RaysumLaunch& L, const ViewGeom& g, const Ar
 
 }  // namespace
 
-// per-view values, computed once per CTA by one thread (FP64 is 1/64 of the
-// FP32 rate on this GPU)
-struct ViewShared {
-  ViewGeom g;
-  ArcFrame af;
-  double ca0, sa0;
-};
+// One thread per (phantom, view, element, ray sample) record; FP64 is 1/64 of
+// the FP32 rate on this GPU and a warp instruction costs the same with one lane
+// active or all, so the set-up runs apart from the rays in full warps.
+// Records of phantom z start at elemOffset[z] * nViews * nSub.
+template <int GEOM>
+__global__ void __launch_bounds__(128) raysum_setup_kernel(RaysumLaunch L) {
+  const int nSub = (GEOM == kParallel) ? L.nSample : 1;
+  const int z = blockIdx.y;
+  int off = 0, nElem = L.nElem;
+  if (L.elemOffset) {
+    off = L.elemOffset[z];
+    nElem = L.elemOffset[z + 1] - off;
+  }
+  const int per = nElem * nSub;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= L.nViews * per) return;
+  const int view = idx / per, ks = idx % per;
+  ElemView* rec = static_cast<ElemView*>(L.records) + (size_t)off * L.nViews * nSub;
+  setup_element<GEOM>(L, L.views[view], L.sdirs, L.elems[off + ks / nSub], ks % nSub, rec[idx]);
+}
 
 template <int GEOM>
 __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
   extern __shared__ __align__(16) ElemView ev[];
-  __shared__ ViewShared vs;
   const int view = blockIdx.x;
   const int nS = L.nSample;
   const int nSub = (GEOM == kParallel) ? nS : 1;
   const PElem* elems = L.elems;
-  int nElem = L.nElem;
+  int off = 0, nElem = L.nElem;
   float* sino = L.sino + (size_t)blockIdx.y * L.sliceStride;
   if (L.elemOffset) {
-    elems += L.elemOffset[blockIdx.y];
-    nElem = L.elemOffset[blockIdx.y + 1] - L.elemOffset[blockIdx.y];
+    off = L.elemOffset[blockIdx.y];
+    nElem = L.elemOffset[blockIdx.y + 1] - off;
+    elems += off;
   }
-  if (threadIdx.x == 0) {
-    const ViewPos vp = L.views[view];
-    view_geom<GEOM>(L, vp, vs.g);
-    vs.af = ArcFrame{};
-    vs.ca0 = 1.0;
-    vs.sa0 = 0.0;
-    if (GEOM == kEquiangular) {
-      const double mid = vs.g.alpha0 + 0.5 * (L.nDet * L.nSample - 1) * vs.g.delta;
-      sincos(vs.g.alpha0, &vs.af.s0, &vs.af.c0);
-      sincos(mid, &vs.af.sm, &vs.af.cm);
-      vs.af.midRel = mid - vs.g.alpha0;
-      vs.af.invDelta = 1.0 / vs.g.delta;
-      vs.ca0 = vs.af.c0;
-      vs.sa0 = vs.af.s0;
-    }
+  const RayView& g = L.views[view];
+  // this view's element records, as 16-byte words
+  {
+    const int4* src = reinterpret_cast<const int4*>(static_cast<const ElemView*>(L.records) +
+                                                    (size_t)off * L.nViews * nSub +
+                                                    (size_t)view * nElem * nSub);
+    int4* dst = reinterpret_cast<int4*>(ev);
+    const int words = nElem * nSub * (int)(sizeof(ElemView) / 16);
+    for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
   }
-  __syncthreads();
-  const ViewGeom& g = vs.g;
   float2* sdir = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(ev) +
                                            dir_table_offset(L.nElem * nSub));   // per sub-sample
-  for (int k = threadIdx.x; k < nElem * nSub; k += blockDim.x)
-    setup_element<GEOM>(L, g, vs.af, elems[k / nSub], k % nSub, ev[k]);
-  if (GEOM == kParallel) {
-    for (int i = threadIdx.x; i < nS; i += blockDim.x) {
-      double drx = (g.D0x + i * g.dDx) - g.S0x, dry = (g.D0y + i * g.dDy) - g.S0y;
-      double inv = 1.0 / sqrt(drx * drx + dry * dry);
-      sdir[i] = make_float2((float)(drx * inv), (float)(dry * inv));
-    }
-  }
+  if (GEOM == kParallel)
+    for (int i = threadIdx.x; i < nS; i += blockDim.x) sdir[i] = L.sdirs[(size_t)view * nS + i];
   __syncthreads();
 
-  // FP32 copies of the per-ray affine quantities
-  const float rsx = (float)(g.D0x - g.S0x), rsy = (float)(g.D0y - g.S0y);
-  const float stx = (float)g.dDx, sty = (float)g.dDy;
-  const float hdelta = (float)(0.5 * g.delta);
-  const float fca0 = (float)vs.ca0, fsa0 = (float)vs.sa0;
+  const float rsx = g.rsx, rsy = g.rsy, stx = g.stx, sty = g.sty;
+  const float hdelta = g.hdelta, fca0 = g.ca0, fsa0 = g.sa0, Sx = g.Sx, Sy = g.Sy;
   const float CD = (float)L.centerDetectorLength;
-  const float Sx = (float)g.S0x, Sy = (float)g.S0y;
 
   for (int d = threadIdx.x; d < L.nDet; d += blockDim.x) {
     float sum = 0.f;
@@ -445,6 +406,30 @@ __global__ void unit_pulse_kernel(float* sino, int nViews, int nDet, int pitch, 
     sino[(size_t)(rowOffset + v) * pitch + d] = (d == nDet / 2) ? 1.f : 0.f;
 }
 
+size_t raysum_record_bytes(const RaysumLaunch& L, int totalElems) {
+  const int nSub = (L.geometry == kParallel) ? L.nSample : 1;
+  return sizeof(ElemView) * (size_t)totalElems * L.nViews * nSub;
+}
+
+template <int GEOM>
+static cudaError_t raysum_launch(const RaysumLaunch& L, size_t smem, int nSlices,
+                                 cudaStream_t s) {
+  const int nSub = (GEOM == kParallel) ? L.nSample : 1;
+  const int per = L.nElem * nSub;
+  if (per > 0) {
+    dim3 gs((L.nViews * per + 127) / 128, nSlices);
+    raysum_setup_kernel<GEOM><<<gs, 128, 0, s>>>(L);
+  }
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(raysum_kernel<GEOM>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  dim3 grid(L.nViews, nSlices);
+  raysum_kernel<GEOM><<<grid, 128, smem, s>>>(L);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_raysum(const RaysumLaunch& L, cudaStream_t s) {
   if (L.nViews <= 0) return cudaSuccess;
   int nSub = (L.geometry == kParallel) ? L.nSample : 1;
@@ -453,25 +438,11 @@ cudaError_t launch_raysum(const RaysumLaunch& L, cudaStream_t s) {
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   const int nSlices = L.nSlices > 0 ? L.nSlices : 1;
   if (nSlices > 65535) return cudaErrorInvalidConfiguration;
-  dim3 grid(L.nViews, nSlices), block(128);
   switch (L.geometry) {
-    case kParallel:
-      if (smem > 48 * 1024)
-        cudaFuncSetAttribute(raysum_kernel<kParallel>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      raysum_kernel<kParallel><<<grid, block, smem, s>>>(L);
-      break;
-    case kEquilinear:
-      if (smem > 48 * 1024)
-        cudaFuncSetAttribute(raysum_kernel<kEquilinear>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      raysum_kernel<kEquilinear><<<grid, block, smem, s>>>(L);
-      break;
-    default:
-      if (smem > 48 * 1024)
-        cudaFuncSetAttribute(raysum_kernel<kEquiangular>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      raysum_kernel<kEquiangular><<<grid, block, smem, s>>>(L);
-      break;
+    case kParallel: return raysum_launch<kParallel>(L, smem, nSlices, s);
+    case kEquilinear: return raysum_launch<kEquilinear>(L, smem, nSlices, s);
+    default: return raysum_launch<kEquiangular>(L, smem, nSlices, s);
   }
-  return cudaGetLastError();
 }
 
 cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int rowOffset,
