@@ -89,6 +89,11 @@ SIGNATURES = {
     "ctgpu_helical180li_size": ([C.POINTER(Geometry), _i, _i, C.POINTER(_i)], _i),
     "ctgpu_helical180li": ([C.POINTER(Geometry), _p, _i, _i, _p, _i, _p, C.POINTER(_i), _p], _i),
     "ctgpu_halfscan_feather": ([C.POINTER(Geometry), _p, _i, _i, _p], _i),
+    "ctgpu_helical180li_equilinear_size": ([C.POINTER(Geometry), _i, _i, C.POINTER(_i)], _i),
+    "ctgpu_helical180li_equilinear": ([C.POINTER(Geometry), _p, _i, _i, _p, _i, _p, C.POINTER(_i),
+                                       _p], _i),
+    "ctgpu_halfscan_feather_equilinear": ([C.POINTER(Geometry), _p, _i, _i, _p], _i),
+    "ctgpu_collect_projections_ellipsoids": ([_p, _p, _i, _d, _d, _p, _i, _p, _p], _i),
     "ctgpu_batch_create": ([C.POINTER(BatchProblem), _i, _i, _pp], _i),
     "ctgpu_batch_run": ([_p, _p], _i),
     "ctgpu_batch_shape": ([_p, C.POINTER(_i), C.POINTER(_i)], _i),

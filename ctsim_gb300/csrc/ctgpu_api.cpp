@@ -248,9 +248,14 @@ struct ctgpu_scanner {
   size_t d_belems_cap = 0;
   int* d_boffs = nullptr;
   size_t d_boffs_cap = 0;
+  // collect_projections_ellipsoids: per-view cross-sections, ellipsoid z extents
+  PElem* d_velems = nullptr;
+  size_t d_velems_cap = 0;
+  double2* d_zc = nullptr;
+  size_t d_zc_cap = 0;
   ~ctgpu_scanner() {
     for (void* p : {(void*)d_views, (void*)d_sino, (void*)d_belems, (void*)d_boffs,
-                    (void*)d_sdirs, (void*)d_records})
+                    (void*)d_sdirs, (void*)d_records, (void*)d_velems, (void*)d_zc})
       if (p) cudaFree(p);
   }
 };
@@ -703,6 +708,63 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   return ok();
 }
 
+int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ell, int n, double z0,
+                                         double dz, float* d_sino, int pitch, double* h_angles,
+                                         void* stream) {
+  if (!s || !d_sino || (n > 0 && !ell) || n < 0) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (pitch < s->nDet) return fail(CTGPU_ERR_INVALID, "sinogram pitch smaller than nDet");
+  for (int j = 0; j < n; j++)
+    if (!(ell[8 * j + 3] > 0 && ell[8 * j + 4] > 0 && ell[8 * j + 5] > 0))
+      return fail(CTGPU_ERR_INVALID, "ellipsoid " + std::to_string(j) + ": semi-axes must be positive");
+  cudaStream_t st = (cudaStream_t)stream;
+  scanner_views(s, 0, s->nView, 0);
+  if (h_angles)
+    for (int v = 0; v < s->nView; v++) h_angles[v] = s->views[v].angle;
+  // ellipsoid j as the 2-D ellipse of its largest cross-section, in the
+  // reference's list order (last added first), with its z extent
+  std::vector<PElem> base(n > 0 ? n : 1);
+  std::vector<double2> zc(n > 0 ? n : 1);
+  for (int j = 0; j < n; j++) {
+    const double* e = ell + 8 * j;
+    base[n - 1 - j] = make_elem(kEllipse, e[0], e[1], e[3], e[4], e[6], e[7]);
+    zc[n - 1 - j] = make_double2(e[2], e[5]);
+  }
+  CUDA_TRY(ensure_device(s->d_belems, s->d_belems_cap, base.size()));
+  CUDA_TRY(ensure_device(s->d_zc, s->d_zc_cap, zc.size()));
+  CUDA_TRY(ensure_device(s->d_velems, s->d_velems_cap, (size_t)(n > 0 ? n : 1) * s->nView));
+  CUDA_TRY(cudaMemcpyAsync(s->d_belems, base.data(), sizeof(PElem) * base.size(),
+                           cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(s->d_zc, zc.data(), sizeof(double2) * zc.size(),
+                           cudaMemcpyHostToDevice, st));
+  CUDA_TRY(launch_ellipsoid_sections(s->d_belems, s->d_zc, n, s->nView, z0, dz, s->d_velems, st));
+  CUDA_TRY(upload_ray_views(s, s->nView, st));
+  RaysumLaunch L{};
+  L.geometry = s->geometry;
+  L.nDet = s->nDet;
+  L.nSample = s->nSample;
+  L.nElem = n;
+  L.nViews = s->nView;
+  L.pitch = pitch;
+  L.rowOffset = 0;
+  L.centerDetectorLength = s->centerDetectorLength;
+  L.angularDetLen = s->angularDetLen;
+  L.angularDetInc = s->angularDetInc;
+  L.elems = s->d_velems;
+  L.views = s->d_views;
+  L.sdirs = s->d_sdirs;
+  L.sino = d_sino;
+  L.status = status_pointer();
+  L.elemsPerView = 1;
+  // records: one per (view, ellipsoid, ray sample), as for nView x n elements
+  CUDA_TRY(ensure_device(s->d_records, s->d_records_cap, raysum_record_bytes(L, n)));
+  L.records = s->d_records;
+  cudaError_t e = launch_raysum(L, st);
+  if (e == cudaErrorInvalidValue)
+    return fail(CTGPU_ERR_UNSUPPORTED, "too many ellipsoids x rays per detector for one CTA");
+  CUDA_TRY(e);
+  return ok();
+}
+
 int ctgpu_collect_projections_host(ctgpu_scanner* s, const ctgpu_phantom* p, int startView,
                                    int nViews, int offsetView, int storageOffset, float* h_sino,
                                    double* h_angles) {
@@ -1125,10 +1187,15 @@ int ctgpu_recon_project(ctgpu_recon* r, const float* d_image, const double* h_an
 }
 
 // ----------------------------------------------------------------- helical --
+// eql: the equilinear restatement (true fan angles), which the reference does
+// not have; otherwise the reference's checks and messages (projections.cpp:203-229)
 static int helical_check(const ctgpu_geometry* g, int nViewIn, int interpView, int* last,
-                         int* offset) {
+                         int* offset, bool eql) {
   if (!g) return fail(CTGPU_ERR_INVALID, "null geometry");
-  if (g->geometry != kEquiangular) {   // projections.cpp:203-229
+  if (eql) {
+    if (g->geometry != kEquilinear)
+      return fail(CTGPU_ERR_INVALID, "the equilinear 180LI needs equilinear projections");
+  } else if (g->geometry != kEquiangular) {
     if (g->geometry == kParallel) return fail(CTGPU_ERR_INVALID, "Helical 180LI not yet implemented for PARALLEL geometry");
     if (g->geometry == kEquilinear) return fail(CTGPU_ERR_INVALID, "Helical 180LI not yet implemented for EQUILINEAR geometry");
     return fail(CTGPU_ERR_INVALID, "Invalid geometry in projection data file");
@@ -1148,18 +1215,19 @@ static int helical_check(const ctgpu_geometry* g, int nViewIn, int interpView, i
   return ok();
 }
 
-int ctgpu_helical180li_size(const ctgpu_geometry* g, int nViewIn, int interpView, int* nOut) {
+static int helical_size(const ctgpu_geometry* g, int nViewIn, int interpView, int* nOut, bool eql) {
   int last, off;
-  int rc = helical_check(g, nViewIn, interpView, &last, &off);
+  int rc = helical_check(g, nViewIn, interpView, &last, &off, eql);
   if (rc) return rc;
   if (nOut) *nOut = last + 1;
   return ok();
 }
 
-int ctgpu_helical180li(const ctgpu_geometry* g, const float* d_in, int nViewIn, int interpView,
-                       float* d_out, int pitch, double* h_angles, int* nOut, void* stream) {
+static int helical_run(const ctgpu_geometry* g, const float* d_in, int nViewIn, int interpView,
+                       float* d_out, int pitch, double* h_angles, int* nOut, void* stream,
+                       bool eql) {
   int last, off;
-  int rc = helical_check(g, nViewIn, interpView, &last, &off);
+  int rc = helical_check(g, nViewIn, interpView, &last, &off, eql);
   if (rc) return rc;
   if (!d_in || !d_out || pitch < g->n_det) return fail(CTGPU_ERR_INVALID, "bad buffers");
   HelicalLaunch L{};
@@ -1171,6 +1239,8 @@ int ctgpu_helical180li(const ctgpu_geometry* g, const float* d_in, int nViewIn, 
   L.dbeta = g->rot_inc;
   L.dgamma = g->det_inc;
   L.fan = g->fan_beam_angle;
+  L.equilinear = eql ? 1 : 0;
+  L.sdl = g->source_detector_length;
   L.in = d_in;
   L.out = d_out;
   L.status = status_pointer();
@@ -1181,14 +1251,16 @@ int ctgpu_helical180li(const ctgpu_geometry* g, const float* d_in, int nViewIn, 
   return ok();
 }
 
-int ctgpu_halfscan_feather(const ctgpu_geometry* g, float* d_data, int nView, int pitch,
-                           void* stream) {
+static int feather_run(const ctgpu_geometry* g, float* d_data, int nView, int pitch, void* stream,
+                       bool eql) {
   if (!g || !d_data) return fail(CTGPU_ERR_INVALID, "null argument");
   double dbeta = g->rot_inc, fan = g->fan_beam_angle;
   if (nView != (int)((kPi + fan) / dbeta) + 1)   // projections.cpp:377-389
     return fail(CTGPU_ERR_INVALID, "Data set does seem have enough data to be a halfscan data set");
   if (g->geometry == kParallel) return fail(CTGPU_ERR_INVALID, "HalfScanFeather not yet implemented for PARALLEL geometry");
   if (g->geometry != kEquiangular && g->geometry != kEquilinear) return fail(CTGPU_ERR_INVALID, "Invalid geometry");
+  if (eql && g->geometry != kEquilinear)
+    return fail(CTGPU_ERR_INVALID, "the equilinear feathering needs equilinear projections");
   cudaStream_t st = (cudaStream_t)stream;
   float* tmp = nullptr;
   size_t bytes = sizeof(float) * (size_t)nView * pitch;
@@ -1202,6 +1274,8 @@ int ctgpu_halfscan_feather(const ctgpu_geometry* g, float* d_data, int nView, in
   L.dbeta = dbeta;
   L.dgamma = g->det_inc;
   L.fan = fan;
+  L.equilinear = eql ? 1 : 0;
+  L.sdl = g->source_detector_length;
   L.in = tmp;
   L.out = d_data;
   L.status = status_pointer();
@@ -1209,6 +1283,36 @@ int ctgpu_halfscan_feather(const ctgpu_geometry* g, float* d_data, int nView, in
   cudaFreeAsync(tmp, st);
   CUDA_TRY(e);
   return ok();
+}
+
+int ctgpu_helical180li_size(const ctgpu_geometry* g, int nViewIn, int interpView, int* nOut) {
+  return helical_size(g, nViewIn, interpView, nOut, false);
+}
+
+int ctgpu_helical180li(const ctgpu_geometry* g, const float* d_in, int nViewIn, int interpView,
+                       float* d_out, int pitch, double* h_angles, int* nOut, void* stream) {
+  return helical_run(g, d_in, nViewIn, interpView, d_out, pitch, h_angles, nOut, stream, false);
+}
+
+int ctgpu_halfscan_feather(const ctgpu_geometry* g, float* d_data, int nView, int pitch,
+                           void* stream) {
+  return feather_run(g, d_data, nView, pitch, stream, false);
+}
+
+int ctgpu_helical180li_equilinear_size(const ctgpu_geometry* g, int nViewIn, int interpView,
+                                       int* nOut) {
+  return helical_size(g, nViewIn, interpView, nOut, true);
+}
+
+int ctgpu_helical180li_equilinear(const ctgpu_geometry* g, const float* d_in, int nViewIn,
+                                  int interpView, float* d_out, int pitch, double* h_angles,
+                                  int* nOut, void* stream) {
+  return helical_run(g, d_in, nViewIn, interpView, d_out, pitch, h_angles, nOut, stream, true);
+}
+
+int ctgpu_halfscan_feather_equilinear(const ctgpu_geometry* g, float* d_data, int nView,
+                                      int pitch, void* stream) {
+  return feather_run(g, d_data, nView, pitch, stream, true);
 }
 
 }  // extern "C"

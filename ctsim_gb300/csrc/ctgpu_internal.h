@@ -66,6 +66,9 @@ struct RaysumLaunch {
   int nSlices;
   const int* elemOffset;
   size_t sliceStride;   // floats between the sinograms
+  // one element list per view (3-D phantoms): view v's nElem elements start
+  // at elems + v * nElem; an element of type < 0 is absent from that view
+  int elemsPerView;
 };
 
 // Filter: out[v][n] = sum_i (w[i] * in[v][i]) * taps[n - i + nDet - 1]
@@ -101,6 +104,10 @@ struct BackprojLaunch {
 struct HelicalLaunch {
   int nDet, nViewIn, nViewOut, offsetView, pitch;
   double dbeta, dgamma, fan;
+  // equilinear restatement: a detector's fan angle is atan(pos / sdl), pos
+  // = (id - (nDet-1)/2) * dgamma (no reference counterpart)
+  int equilinear;
+  double sdl;
   const float* in;    // original data
   float* out;
   unsigned int* status;
@@ -119,6 +126,11 @@ cudaError_t status_read_and_clear(unsigned int* value);
 
 // kernel entry wrappers (defined in the .cu files)
 cudaError_t launch_raysum(const RaysumLaunch& L, cudaStream_t s);
+// Per-view cross-sections of ellipsoids: base[k] is ellipsoid k as a 2-D
+// ellipse at its full semi-axes, zc[k] its (z centre, z semi-axis); out[v][k]
+// is the ellipse cut at z0 + v dz, scaled about its centre, or absent.
+cudaError_t launch_ellipsoid_sections(const PElem* base, const double2* zc, int n, int nViews,
+                                      double z0, double dz, PElem* out, cudaStream_t s);
 // scratch of launch_raysum: one record per (phantom, view, element, ray sample)
 size_t raysum_record_bytes(const RaysumLaunch& L, int totalElems);
 cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int rowOffset,

@@ -10,6 +10,12 @@
 // evaluates the same FP64 region tests and weights, and adds them in the
 // reference's order with the reference's FP32 rounding, so the result is
 // bit-identical and deterministic.
+//
+// Equilinear restatement (no reference counterpart; the reference refuses
+// that geometry, projections.cpp:214-218): the same algorithm with each
+// detector's true fan angle gamma = atan(pos / SDL), pos its distance from
+// the integer detector centre (projections.cpp:1366-1370 maps the equilinear
+// detector to fan angles the same way).
 #include "ctgpu_internal.h"
 
 namespace ctgpu {
@@ -17,6 +23,12 @@ namespace ctgpu {
 namespace {
 
 __device__ __forceinline__ int nearest_int(double x) { return x > 0 ? (int)(x + 0.5) : (int)(x - 0.5); }
+
+// fan angle of detector id (projections.cpp:247: integer centre (nDet-1)/2)
+__device__ __forceinline__ double det_gamma(const HelicalLaunch& L, int id) {
+  const double pos = (id - (L.nDet - 1) / 2) * L.dgamma;
+  return L.equilinear ? atan(pos / L.sdl) : pos;
+}
 
 // weight of input ray (iv, id) in the 180LI sum; false outside regions 2-7
 // (projections.cpp:306-350)
@@ -38,7 +50,7 @@ __device__ bool li_weight(double beta, double gamma, double fan, double* w) {
 __global__ void helical180li_kernel(HelicalLaunch L) {
   const int vo = blockIdx.x;                  // output view
   const int nDet = L.nDet;
-  const double dbeta = L.dbeta, dgamma = L.dgamma, fan = L.fan, PI = kPi;
+  const double dbeta = L.dbeta, fan = L.fan, PI = kPi;
   const int last = L.nViewOut - 1, lastAcq = 2 * last;
   for (int dO = threadIdx.x; dO < nDet; dO += blockDim.x) {
     float o = 0.f;
@@ -46,7 +58,7 @@ __global__ void helical180li_kernel(HelicalLaunch L) {
     {
       int iv = vo, id = dO;
       double beta = iv * dbeta;
-      double gamma = (id - (nDet - 1) / 2) * dgamma;
+      double gamma = det_gamma(L, id);
       double w;
       if (beta < PI + fan && li_weight(beta, gamma, fan, &w))
         o = (float)((double)o + w * (double)L.in[(size_t)(iv + L.offsetView) * L.pitch + id]);
@@ -54,13 +66,13 @@ __global__ void helical180li_kernel(HelicalLaunch L) {
     // complementary ray: id = nDet-1-dO, nearest(iv + (2 gamma - pi)/dbeta) == vo
     {
       int id = nDet - 1 - dO;
-      double gamma = (id - (nDet - 1) / 2) * dgamma;
-      int guess = (int)floor(vo - (2 * (id - (nDet - 1) / 2) * dgamma - PI) / dbeta);
+      double gamma = det_gamma(L, id);
+      int guess = (int)floor(vo - (2 * gamma - PI) / dbeta);
       for (int iv = guess - 2; iv <= guess + 2; iv++) {
         if (iv < 0 || iv > lastAcq) continue;
         double beta = iv * dbeta;
         if (beta < PI + fan) continue;
-        int nv = nearest_int(((iv * dbeta) + 2 * (id - (nDet - 1) / 2) * dgamma - PI) / dbeta);
+        int nv = nearest_int(((iv * dbeta) + 2 * gamma - PI) / dbeta);
         if (nv != vo) continue;
         double w;
         if (li_weight(beta, gamma, fan, &w))
@@ -87,28 +99,28 @@ __device__ bool feather_w1(double beta1, double gamma1, double fan, double* w1) 
 __global__ void halfscan_feather_kernel(HelicalLaunch L) {
   const int v = blockIdx.x;
   const int nDet = L.nDet, nView = L.nViewOut;
-  const double dbeta = L.dbeta, dgamma = L.dgamma, fan = L.fan, PI = kPi;
+  const double dbeta = L.dbeta, fan = L.fan, PI = kPi;
   const double sf = nView * L.dbeta / PI;
   for (int d = threadIdx.x; d < nDet; d += blockDim.x) {
     float x = L.in[(size_t)v * L.pitch + d];
     double beta = v * dbeta;
-    double gamma = (d - (nDet - 1) / 2) * dgamma;
+    double gamma = det_gamma(L, d);
     if (beta >= PI - 2 * gamma) {
       // redundant sample: keeps weight w2 = 1 - w1 of its complement
-      int iv1 = nearest_int(((v * dbeta) + 2 * (d - (nDet - 1) / 2) * dgamma - PI) / dbeta);
+      int iv1 = nearest_int(((v * dbeta) + 2 * gamma - PI) / dbeta);
       double w1;
       if (!feather_w1(iv1 * dbeta, -gamma, fan, &w1)) { atomicOr(L.status, kStatusFeatherRange); w1 = 0; }
       x = (float)((double)x * (1 - w1));
     } else {
       // complement target of the redundant sample (iv2, nDet-1-d), if any
       int id2 = nDet - 1 - d;
-      double gamma2 = (id2 - (nDet - 1) / 2) * dgamma;
+      double gamma2 = det_gamma(L, id2);
       int guess = (int)floor(v + (PI - 2 * gamma2) / dbeta);
       for (int iv2 = guess - 2; iv2 <= guess + 2; iv2++) {
         if (iv2 < 0 || iv2 >= nView) continue;
         double beta2 = iv2 * dbeta;
         if (!(beta2 >= PI - 2 * gamma2)) continue;
-        int iv1 = nearest_int(((iv2 * dbeta) + 2 * (id2 - (nDet - 1) / 2) * dgamma - PI) / dbeta);
+        int iv1 = nearest_int(((iv2 * dbeta) + 2 * gamma2 - PI) / dbeta);
         if (iv1 != v) continue;
         double w1;
         if (!feather_w1(v * dbeta, -gamma2, fan, &w1)) { atomicOr(L.status, kStatusFeatherRange); w1 = 0; }

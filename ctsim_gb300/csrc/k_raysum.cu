@@ -213,6 +213,10 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
   e.kB = 0.f;
   e.tcI = 0;
   e.tcF = 0.f;
+  if (pe.type < 0) {   // absent from this view (3-D phantom cross-section)
+    e.live = 0;
+    return;
+  }
   if (GEOM == kParallel) {
     // ray direction of sub-sample `sub` (independent of the detector index)
     double rx = (g.D0x + sub * g.dDx) - g.S0x, ry = (g.D0y + sub * g.dDy) - g.S0y;
@@ -286,7 +290,8 @@ __global__ void __launch_bounds__(128) raysum_setup_kernel(RaysumLaunch L) {
   if (idx >= L.nViews * per) return;
   const int view = idx / per, ks = idx % per;
   ElemView* rec = static_cast<ElemView*>(L.records) + (size_t)off * L.nViews * nSub;
-  setup_element<GEOM>(L, L.views[view], L.sdirs, L.elems[off + ks / nSub], ks % nSub, rec[idx]);
+  const PElem* el = L.elems + off + (L.elemsPerView ? (size_t)view * nElem : 0);
+  setup_element<GEOM>(L, L.views[view], L.sdirs, el[ks / nSub], ks % nSub, rec[idx]);
 }
 
 template <int GEOM>
@@ -303,6 +308,7 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
     nElem = L.elemOffset[blockIdx.y + 1] - off;
     elems += off;
   }
+  if (L.elemsPerView) elems += (size_t)view * nElem;
   const RayView& g = L.views[view];
   // this view's element records, as 16-byte words
   {
@@ -443,6 +449,44 @@ cudaError_t launch_raysum(const RaysumLaunch& L, cudaStream_t s) {
     case kEquilinear: return raysum_launch<kEquilinear>(L, smem, nSlices, s);
     default: return raysum_launch<kEquiangular>(L, smem, nSlices, s);
   }
+}
+
+__global__ void ellipsoid_section_kernel(const PElem* base, const double2* zc, int n, int nViews,
+                                         double z0, double dz, PElem* out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * nViews) return;
+  const int v = idx / n, k = idx % n;
+  PElem e = base[k];
+  const double d = (z0 + v * dz - zc[k].x) / zc[k].y;
+  if (!(fabs(d) < 1.0)) {
+    e.type = -1;
+  } else {
+    const double sc = sqrt((1.0 - d) * (1.0 + d));
+    e.u *= sc;
+    e.v *= sc;
+    e.bx0 = e.cx + sc * (e.bx0 - e.cx);
+    e.bx1 = e.cx + sc * (e.bx1 - e.cx);
+    e.by0 = e.cy + sc * (e.by0 - e.cy);
+    e.by1 = e.cy + sc * (e.by1 - e.cy);
+    const double hx = 0.5 * (e.bx1 - e.bx0), hy = 0.5 * (e.by1 - e.by0);
+    e.dcbx = (float)(0.5 * (e.bx0 + e.bx1) - e.cx);
+    e.dcby = (float)(0.5 * (e.by0 + e.by1) - e.cy);
+    e.hx = (float)hx;
+    e.hy = (float)hy;
+    e.rbox = (float)(sqrt(hx * hx + hy * hy) * (1.0 + 1e-5) + 1e-7);
+    e.rin = (float)(fmin(hx, hy) - 2e-5 * (hx + hy) - 1e-7);
+  }
+  out[idx] = e;
+}
+
+cudaError_t launch_ellipsoid_sections(const PElem* base, const double2* zc, int n, int nViews,
+                                      double z0, double dz, PElem* out, cudaStream_t s) {
+  if (n <= 0 || nViews <= 0) return cudaSuccess;
+  const long long total = (long long)n * nViews;
+  if (total > (1LL << 31) - 256) return cudaErrorInvalidValue;
+  ellipsoid_section_kernel<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(base, zc, n, nViews, z0,
+                                                                          dz, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int rowOffset,

@@ -228,24 +228,41 @@ class BatchPlan:
             self._h = None
 
 
-def helical180li(geometry, sino, interp_view=-1, stream=None):
-    """Projections::Helical180LI on a device sinogram; returns (out, angles)."""
+def helical180li(geometry, sino, interp_view=-1, stream=None, equilinear=False):
+    """Projections::Helical180LI on a device sinogram; returns (out, angles).
+    equilinear=True: the equilinear restatement (true detector fan angles),
+    which the reference does not have."""
     torch = _torch()
     n = C.c_int()
-    check(lib().ctgpu_helical180li_size(C.byref(geometry), sino.shape[0], interp_view, C.byref(n)))
+    size = lib().ctgpu_helical180li_equilinear_size if equilinear else lib().ctgpu_helical180li_size
+    run = lib().ctgpu_helical180li_equilinear if equilinear else lib().ctgpu_helical180li
+    check(size(C.byref(geometry), sino.shape[0], interp_view, C.byref(n)))
     out = torch.empty((n.value, sino.shape[1]), dtype=torch.float32, device=sino.device)
     ang = np.zeros(n.value, np.float64)
-    check(lib().ctgpu_helical180li(C.byref(geometry), _ptr(sino), sino.shape[0], interp_view,
-                                   _ptr(out), sino.shape[1], ang.ctypes.data_as(C.c_void_p),
-                                   C.byref(n), stream_handle(stream)))
+    check(run(C.byref(geometry), _ptr(sino), sino.shape[0], interp_view, _ptr(out),
+              sino.shape[1], ang.ctypes.data_as(C.c_void_p), C.byref(n), stream_handle(stream)))
     return out, ang
 
 
-def halfscan_feather(geometry, sino, stream=None):
-    """Projections::HalfScanFeather, in place on a device sinogram."""
-    check(lib().ctgpu_halfscan_feather(C.byref(geometry), _ptr(sino), sino.shape[0],
-                                       sino.shape[1], stream_handle(stream)))
+def halfscan_feather(geometry, sino, stream=None, equilinear=False):
+    """Projections::HalfScanFeather, in place on a device sinogram (equilinear:
+    the restatement with true detector fan angles)."""
+    fn = lib().ctgpu_halfscan_feather_equilinear if equilinear else lib().ctgpu_halfscan_feather
+    check(fn(C.byref(geometry), _ptr(sino), sino.shape[0], sino.shape[1], stream_handle(stream)))
     return sino
+
+
+def raysums_ellipsoids(scanner, ellipsoids, z0, dz, sino, stream=None):
+    """Helical scan of a 3-D ellipsoid phantom (rows cx, cy, cz, a, b, c,
+    rot_deg, atten): view v sees the cross-section at z0 + v dz.  Returns the
+    view angles."""
+    g = scanner.geometry()
+    ell = np.ascontiguousarray(ellipsoids, np.float64).reshape(-1, 8)
+    ang = np.zeros(g.n_view, np.float64)
+    check(lib().ctgpu_collect_projections_ellipsoids(
+        scanner._h, ell.ctypes.data_as(C.c_void_p), ell.shape[0], float(z0), float(dz),
+        _ptr(sino), sino.shape[1], ang.ctypes.data_as(C.c_void_p), stream_handle(stream)))
+    return ang
 
 
 def _to_device(a):

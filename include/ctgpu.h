@@ -126,6 +126,19 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
                                     int n_phantoms, float* d_sinos, int sino_pitch,
                                     long long sino_slice_stride, double* h_view_angles,
                                     void* stream);
+/* Helical scan of a 3-D phantom of n_ellipsoids ellipsoids, all n_view views
+ * of the scanner (its geometry is that of a 2-D phantom; make it from the
+ * ellipsoids' largest cross-sections).  View v sees the phantom's
+ * cross-section at z = z0 + v * dz_per_view: ellipsoid k, ellipsoids[8k..8k+7]
+ * = cx, cy, cz, a, b, c, rotation about z (degrees), attenuation, contributes
+ * the ellipse (cx, cy, a s, b s) with s = sqrt(1 - ((z - cz)/c)^2) while
+ * |z - cz| < c.  No reference counterpart (CTSim's phantoms are 2-D); the
+ * views are projected as Scanner::projectSingleView does
+ * (scanner.cpp:445-533). */
+int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ellipsoids,
+                                         int n_ellipsoids, double z0, double dz_per_view,
+                                         float* d_sino, int sino_pitch, double* h_view_angles,
+                                         void* stream);
 void ctgpu_scanner_destroy(ctgpu_scanner* s);
 
 /* ------------------------------------------------------------------------ */
@@ -258,6 +271,18 @@ int ctgpu_helical180li(const ctgpu_geometry* g, const float* d_in, int n_view_in
 /* in place on d_data [n_view][pitch] */
 int ctgpu_halfscan_feather(const ctgpu_geometry* g, float* d_data, int n_view, int pitch,
                            void* stream);
+/* The equilinear restatement of Helical180LI and HalfScanFeather (no
+ * reference counterpart: the reference refuses equilinear data,
+ * projections.cpp:214-218): the same algorithm with each detector's true fan
+ * angle gamma = atan(pos / SDL), pos = (id - (n_det-1)/2) * det_inc; needs
+ * equilinear projections.  Arguments as the equiangular entry points. */
+int ctgpu_helical180li_equilinear_size(const ctgpu_geometry* g, int n_view_in, int interp_view,
+                                       int* n_view_out);
+int ctgpu_helical180li_equilinear(const ctgpu_geometry* g, const float* d_in, int n_view_in,
+                                  int interp_view, float* d_out, int pitch,
+                                  double* h_out_angles, int* n_view_out, void* stream);
+int ctgpu_halfscan_feather_equilinear(const ctgpu_geometry* g, float* d_data, int n_view,
+                                      int pitch, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Allocation-free variant                                                   */

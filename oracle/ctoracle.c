@@ -573,6 +573,62 @@ void ora_collect_projections(const ora_scanner* s, const ora_phantom* p, int iSt
   free(vp);
 }
 
+/* Helical scan of a 3-D ellipsoid phantom: a restatement with no reference
+ * counterpart (CTSim's phantoms are 2-D).  View v of the scanner (positions
+ * as collectProjections over all views, scanner.cpp:295-419) sees the
+ * phantom's cross-section at z = z0 + v dz: ellipsoid k (cx, cy, cz, a, b, c,
+ * rotation about z in degrees, attenuation) contributes the ellipse
+ * (cx, cy, a s, b s) with s = sqrt(1 - ((z - cz)/c)^2) when |z - cz| < c,
+ * added in ellipsoid order (so the list order is the reference's, last
+ * added first), and the view is projected as projectSingleView does. */
+void ora_collect_ellipsoids(const ora_scanner* s, const double* ell, int n, double z0, double dz,
+                            double* sino, double* viewAngles, int nThreads) {
+  int nv = s->nView;
+  view_pos* vp = malloc((size_t)nv * sizeof(view_pos));
+  double start = 0.0;
+  mtx2 m0, t;
+  m_xlat(m0, -s->xCenter, -s->yCenter);
+  m_rot(t, start); m_mul(m0, t, m0);
+  m_xlat(t, s->xCenter, s->yCenter); m_mul(m0, t, m0);
+  double xd1 = 0, yd1 = 0, xd2 = 0, yd2 = 0;
+  if (s->geometry != ORA_GEOM_EQUIANGULAR) {
+    xd1 = s->xd1; yd1 = s->yd1; xd2 = s->xd2; yd2 = s->yd2;
+    m_apply((const double(*)[3])m0, &xd1, &yd1);
+    m_apply((const double(*)[3])m0, &xd2, &yd2);
+  }
+  double xs1 = s->xs1, ys1 = s->ys1, xs2 = s->xs2, ys2 = s->ys2;
+  m_apply((const double(*)[3])m0, &xs1, &ys1);
+  m_apply((const double(*)[3])m0, &xs2, &ys2);
+  double ang = start;
+  for (int v = 0; v < nv; v++, ang += s->rotInc) {
+    view_pos q = {xs1, ys1, xs2, ys2, xd1, yd1, xd2, yd2, ang};
+    vp[v] = q;
+    m_apply(s->incmtx, &xs1, &ys1);
+    m_apply(s->incmtx, &xs2, &ys2);
+    if (s->geometry != ORA_GEOM_EQUIANGULAR) {
+      m_apply(s->incmtx, &xd1, &yd1);
+      m_apply(s->incmtx, &xd2, &yd2);
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nThreads > 0 ? nThreads : 1)
+  for (int v = 0; v < nv; v++) {
+    ora_phantom p;
+    ora_phantom_init(&p, n > 0 ? n : 1);
+    double z = z0 + v * dz;
+    for (int k = 0; k < n; k++) {
+      const double* e = ell + 8 * k;
+      double d = (z - e[2]) / e[5];
+      if (!(fabs(d) < 1.0)) continue;
+      double sc = sqrt((1.0 - d) * (1.0 + d));
+      ora_phantom_add(&p, ORA_PELEM_ELLIPSE, e[0], e[1], e[3] * sc, e[4] * sc, e[6], e[7]);
+    }
+    project_view(s, &p, &vp[v], &sino[(size_t)v * s->nDet]);
+    if (viewAngles) viewAngles[v] = vp[v].angle;
+    ora_phantom_free(&p);
+  }
+  free(vp);
+}
+
 /* ------------------------------------------------------------------------- */
 /* Signal filters: libctsim/filter.cpp                                      */
 /* ------------------------------------------------------------------------- */
@@ -1225,11 +1281,25 @@ int ora_reconstruct(const ora_geom* g, const float* sino, const double* angles, 
 /* Helical 180LI and half-scan feathering: libctsim/projections.cpp:231-439 */
 /* (FP32 storage with FP64 weights, exactly as the reference)               */
 /* ------------------------------------------------------------------------- */
-int ora_helical180li(const ora_geom* g, const float* in, int nView, int interpView,
-                     float* out, double* outAngles, int* nViewOut) {
-  double dbeta = g->rotInc, dgamma = g->detInc, fan = g->fanBeamAngle;
+/* fan angle of detector id: equiangular (projections.cpp:247, :378) uses the
+ * integer centre (nDet-1)/2 times detInc; the equilinear restatement (no
+ * reference counterpart) maps the same detector position through
+ * atan(pos / SDL) (projections.cpp:1366-1370). */
+static double det_gamma(const ora_geom* g, int id) {
+  double pos = (id - (g->nDet - 1) / 2) * g->detInc;
+  if (g->geometry == ORA_GEOM_EQUILINEAR) return atan(pos / g->sourceDetectorLength);
+  return pos;
+}
+
+/* Projections::Helical180LI_Equiangular (projections.cpp:231-358); with
+ * allowEquilinear, the same algorithm for an equilinear detector. */
+int ora_helical180li_ex(const ora_geom* g, const float* in, int nView, int interpView,
+                        float* out, double* outAngles, int* nViewOut, int allowEquilinear) {
+  double dbeta = g->rotInc, fan = g->fanBeamAngle;
   int nDet = g->nDet, offsetView = 0;
-  if (g->geometry != ORA_GEOM_EQUIANGULAR) return 2;
+  if (!(g->geometry == ORA_GEOM_EQUIANGULAR ||
+        (allowEquilinear && g->geometry == ORA_GEOM_EQUILINEAR)))
+    return 2;
   if (nView < (int)((2 * (O_PI + fan)) / dbeta) - 1) return 1;
   if (interpView < 0) interpView = (int)((O_PI + fan) / dbeta);
   else {
@@ -1244,12 +1314,12 @@ int ora_helical180li(const ora_geom* g, const float* in, int nView, int interpVi
   for (int iv = 0; iv <= lastAcq; iv++) {
     double beta = iv * dbeta;
     for (int id = 0; id < nDet; id++) {
-      double gamma = (id - (nDet - 1) / 2) * dgamma;
+      double gamma = det_gamma(g, id);
       int nv, nd;
       if (beta < O_PI + fan) { nd = id; nv = iv; }
       else {
         nd = -id + (nDet - 1);
-        nv = nearest_int(((iv * dbeta) + 2 * (id - (nDet - 1) / 2) * dgamma - O_PI) / dbeta);
+        nv = nearest_int(((iv * dbeta) + 2 * gamma - O_PI) / dbeta);
       }
       if ((beta > fan - 2 * gamma) && (beta < 2 * O_PI + fan - 2 * gamma)) {
         float x = in[(size_t)(iv + offsetView) * nDet + id];
@@ -1273,18 +1343,27 @@ int ora_helical180li(const ora_geom* g, const float* in, int nView, int interpVi
   return 0;
 }
 
-int ora_halfscan_feather(const ora_geom* g, float* data, int nView) {
-  double dbeta = g->rotInc, dgamma = g->detInc, fan = g->fanBeamAngle;
+int ora_helical180li(const ora_geom* g, const float* in, int nView, int interpView,
+                     float* out, double* outAngles, int* nViewOut) {
+  return ora_helical180li_ex(g, in, nView, interpView, out, outAngles, nViewOut, 0);
+}
+
+/* Projections::HalfScanFeather (projections.cpp:369-439).  The reference
+ * takes gamma = (id - (nDet-1)/2) detInc for every fan geometry; with
+ * trueGamma the equilinear detector's fan angle det_gamma() is used instead
+ * (the restatement that goes with ora_helical180li_ex). */
+int ora_halfscan_feather_ex(const ora_geom* g, float* data, int nView, int trueGamma) {
+  double dbeta = g->rotInc, fan = g->fanBeamAngle;
   int nDet = g->nDet;
   if (nView != (int)((O_PI + fan) / dbeta) + 1) return 1;
   if (g->geometry == ORA_GEOM_PARALLEL) return 2;
   for (int iv2 = 0; iv2 < nView; iv2++) {
     double beta2 = iv2 * dbeta;
     for (int id2 = 0; id2 < nDet; id2++) {
-      double gamma2 = (id2 - (nDet - 1) / 2) * dgamma;
+      double gamma2 = trueGamma ? det_gamma(g, id2) : (id2 - (nDet - 1) / 2) * g->detInc;
       if (beta2 >= O_PI - 2 * gamma2) {
         int id1 = (nDet - 1) - id2;
-        int iv1 = nearest_int(((iv2 * dbeta) + 2 * (id2 - (nDet - 1) / 2) * dgamma - O_PI) / dbeta);
+        int iv1 = nearest_int(((iv2 * dbeta) + 2 * gamma2 - O_PI) / dbeta);
         float* d2 = &data[(size_t)iv2 * nDet + id2];
         float* d1 = &data[(size_t)iv1 * nDet + id1];
         *d1 = *d2;
@@ -1303,6 +1382,10 @@ int ora_halfscan_feather(const ora_geom* g, float* data, int nView) {
   double sf = nView * g->rotInc / O_PI;
   for (size_t i = 0; i < (size_t)nView * nDet; i++) data[i] *= sf;
   return 0;
+}
+
+int ora_halfscan_feather(const ora_geom* g, float* data, int nView) {
+  return ora_halfscan_feather_ex(g, data, nView, 0);
 }
 
 /* ------------------------------------------------------------------------- */

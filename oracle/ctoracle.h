@@ -85,6 +85,10 @@ void ora_collect_projections(const ora_scanner* s, const ora_phantom* p, int iSt
                              int iNumViews, int iOffsetView, int iStorageOffset, double* sino,
                              double* viewAngles, int nThreads);
 double ora_raysum(const ora_phantom* p, double x1, double y1, double x2, double y2);
+/* helical scan of a 3-D ellipsoid phantom (restatement only); ell[8k..8k+7] =
+ * cx, cy, cz, a, b, c, rot_deg, atten; view v sees z = z0 + v dz */
+void ora_collect_ellipsoids(const ora_scanner* s, const double* ell, int n, double z0, double dz,
+                            double* sino, double* viewAngles, int nThreads);
 
 /* ---- filtering ---- */
 int  ora_filter_id(const char* name);
@@ -116,6 +120,10 @@ int  ora_reconstruct(const ora_geom* g, const float* sino, const double* viewAng
 int  ora_helical180li(const ora_geom* g, const float* in, int nViewIn, int interpView,
                       float* out, double* outAngles, int* nViewOut);
 int  ora_halfscan_feather(const ora_geom* g, float* data, int nView);
+/* the same, with the equilinear restatement allowed / the true equilinear fan angle */
+int  ora_helical180li_ex(const ora_geom* g, const float* in, int nViewIn, int interpView,
+                         float* out, double* outAngles, int* nViewOut, int allowEquilinear);
+int  ora_halfscan_feather_ex(const ora_geom* g, float* data, int nView, int trueGamma);
 
 /* ---- rasteriser (phm2if) and pixel-image projector ---- */
 void ora_phantom_to_image(const ora_phantom* p, int nx, int ny, double viewRatio, int nsample,

@@ -87,6 +87,9 @@ def lib():
         _LIB.ora_reconstruct.argtypes = [C.POINTER(Geom), p, p, i, i, i, d, i, i, i, i, i, p, i]
         _LIB.ora_helical180li.argtypes = [C.POINTER(Geom), p, i, i, p, p, C.POINTER(C.c_int)]
         _LIB.ora_halfscan_feather.argtypes = [C.POINTER(Geom), p, i]
+        _LIB.ora_helical180li_ex.argtypes = [C.POINTER(Geom), p, i, i, p, p, C.POINTER(C.c_int), i]
+        _LIB.ora_halfscan_feather_ex.argtypes = [C.POINTER(Geom), p, i, i]
+        _LIB.ora_collect_ellipsoids.argtypes = [C.POINTER(_Scanner), p, i, d, d, p, p, i]
         _LIB.ora_phantom_to_image.argtypes = [C.POINTER(_Phantom), i, i, d, i, p, p, i]
         _LIB.ora_project_image.argtypes = [C.POINTER(Geom), p, i, i, p, i, p, i]
         _LIB.ora_frequency_response.argtypes = [i, d, d, d]
@@ -189,6 +192,19 @@ class Scanner:
         return sino, ang
 
 
+def collect_ellipsoids(scanner, ellipsoids, z0, dz, nthreads=None):
+    """Helical scan of a 3-D ellipsoid phantom (restatement only): view v sees
+    the cross-section at z0 + v dz.  ellipsoids: rows (cx, cy, cz, a, b, c,
+    rot_deg, atten)."""
+    s = scanner._s
+    ell = np.ascontiguousarray(ellipsoids, np.float64).reshape(-1, 8)
+    sino = np.zeros((s.nView, s.nDet), np.float64)
+    ang = np.zeros(s.nView, np.float64)
+    lib().ora_collect_ellipsoids(C.byref(s), _ptr(ell), ell.shape[0], z0, dz, _ptr(sino), _ptr(ang),
+                                 nthreads or nthreads_default())
+    return sino, ang
+
+
 class ProcessSignal:
     def __init__(self, filter_name, method, ndet, det_inc, param=-1.0, generation="direct",
                  zeropad=1, interp_factor=1, geometry="parallel", focal_length=0.0, sdl=0.0):
@@ -255,21 +271,25 @@ def reconstruct(geom, sino, angles, nx, ny, filter_name="abs_bandlimit", param=-
     return img
 
 
-def helical180li(geom, sino, interp_view=-1):
+def helical180li(geom, sino, interp_view=-1, allow_equilinear=False):
+    """Helical180LI; allow_equilinear: the equilinear restatement (no reference
+    counterpart) instead of the reference's refusal."""
     sino = np.ascontiguousarray(sino, np.float32)
     out = np.zeros_like(sino)
     ang = np.zeros(sino.shape[0], np.float64)
     n = C.c_int(0)
-    rc = lib().ora_helical180li(C.byref(geom), _ptr(sino), sino.shape[0], interp_view,
-                                _ptr(out), _ptr(ang), C.byref(n))
+    rc = lib().ora_helical180li_ex(C.byref(geom), _ptr(sino), sino.shape[0], interp_view,
+                                   _ptr(out), _ptr(ang), C.byref(n), int(allow_equilinear))
     if rc != 0:
         raise ValueError("Helical180LI failed: %d" % rc)
     return out[:n.value].copy(), ang[:n.value].copy()
 
 
-def halfscan_feather(geom, sino):
+def halfscan_feather(geom, sino, true_gamma=False):
+    """HalfScanFeather; true_gamma: the equilinear detector's fan angle (the
+    restatement that goes with helical180li(allow_equilinear=True))."""
     data = np.ascontiguousarray(sino, np.float32).copy()
-    rc = lib().ora_halfscan_feather(C.byref(geom), _ptr(data), data.shape[0])
+    rc = lib().ora_halfscan_feather_ex(C.byref(geom), _ptr(data), data.shape[0], int(true_gamma))
     if rc != 0:
         raise ValueError("HalfScanFeather failed: %d" % rc)
     return data
