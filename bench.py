@@ -273,6 +273,70 @@ def batched_uneven(args, torch, cg, device, phantoms, rank):
             "one_plan_after_another": {"value": total_pv / (seq_ms / 1e3), "ms_per_run": seq_ms}}
 
 
+def helical_3d(args, torch, cg, device, phantoms, rank):
+    """The helical workload: 16 seeded ellipsoids over z in [-1, 1], equilinear
+    detector of 1024, 1152 views per rotation, 8 rotations (z advances 0.25
+    per rotation, the ray plane of each view at its own z), 180-degree linear
+    z-interpolation with the equilinear fan angles and half-scan feathering at
+    64 slice positions, then the FBP of the 64 slices at 1024 x 1024 (Shepp
+    filter by FFT, zero-pad 2, linear interpolation) as one ctgpu_batch.
+    Each phase timed with CUDA events over `steps` repetitions."""
+    ell = phantoms.random_ellipsoids(seed=77 + rank, n=16, z_half=1.0)
+    nrot, nvr, ndet, nslice, side = 8, 1152, 1024, 64, 1024
+    nview = nrot * nvr
+    z0, dz = -1.0, 2.0 / nview
+    sc = cg.Scanner(phantoms.make_phantom(phantoms.ellipsoid_footprint(ell)), "equilinear", ndet,
+                    nview, rotAngle=nrot * 2 * np.pi)
+    g = sc.geometry()
+    sino = device.alloc_sinogram(nview, ndet)
+    stream = torch.cuda.current_stream()
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        cg.sync()
+        return a.elapsed_time(b) / reps
+
+    scan_ms = timed(lambda: device.raysums_ellipsoids(sc, ell, z0, dz, sino), args.steps)
+    hplan = device.HelicalPlan(g, nview, equilinear=True, feather=True)
+    last = hplan.n_view_out - 1
+    ivs = np.linspace(last + 1, nview - last - 2, nslice).astype(int)
+    zsino = torch.empty((nslice, hplan.n_view_out, sino.shape[1]), device="cuda")
+    angs = [None]
+
+    def interp():
+        angs[0] = hplan.run(sino, ivs, zsino)[1]
+
+    interp_ms = timed(interp, args.steps)
+    gh = cg.Geometry.from_buffer_copy(g)
+    gh.n_view = hplan.n_view_out
+    probs = [dict(geometry=gh, nx=side, ny=side, sino=zsino[k], angles=angs[0][k],
+                  image=torch.zeros((side, side), device="cuda"), filter_name="shepp",
+                  filter_param=-1.0, filter_method="fft", zeropad=2, interp="linear",
+                  backproj="table") for k in range(nslice)]
+    batch = device.BatchPlan(probs, autotune=True, graph=True)
+    batch.run()
+    fbp_ms = timed(batch.run, args.steps)
+    pv = nslice * side * side * gh.n_view
+    return {"workload": "16 ellipsoids, equilinear 1024 det, 1152 views/rotation x 8, "
+                        "64 slices of 1024x1024, Shepp FFT zero-pad 2",
+            "scan": {"ms": scan_ms, "ray_sums_per_s": nview * ndet / (scan_ms / 1e3),
+                     "ray_element_pairs_per_s": nview * ndet * 16 / (scan_ms / 1e3)},
+            "z_interpolation": {"ms": interp_ms, "slices": nslice,
+                                "launch": "one ctgpu_helical_plan run (180LI + feathering)"},
+            "fbp": {"ms": fbp_ms, "views_per_slice": gh.n_view,
+                    "value": pv / (fbp_ms / 1e3), "unit": UNIT}}
+
+
 def run_gpu(args):
     import torch
     import ctsim_gb300 as cg
@@ -372,6 +436,7 @@ def run_gpu(args):
 
     batched = batched_uneven(args, torch, cg, device, phantoms, rank) \
         if args.batched_problems > 0 else None
+    helical = helical_3d(args, torch, cg, device, phantoms, rank) if args.helical else None
 
     if rank != 0:
         return 0
@@ -430,6 +495,7 @@ def run_gpu(args):
         # backprojection itself for the batch
         "gpu_launches": steps * 4,
         "batched_uneven": batched,
+        "helical": helical,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))
@@ -447,6 +513,8 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--helical", type=int, default=1,
+                    help="measure the helical 3-D workload after the main one (0: skip)")
     ap.add_argument("--batched-problems", type=int, default=64,
                     help="problems of the uneven batch measured after the main workload (0: skip)")
     ap.add_argument("--ref-views", type=int, default=None,

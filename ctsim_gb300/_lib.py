@@ -93,6 +93,10 @@ SIGNATURES = {
     "ctgpu_helical180li_equilinear": ([C.POINTER(Geometry), _p, _i, _i, _p, _i, _p, C.POINTER(_i),
                                        _p], _i),
     "ctgpu_halfscan_feather_equilinear": ([C.POINTER(Geometry), _p, _i, _i, _p], _i),
+    "ctgpu_helical_plan_create": ([C.POINTER(Geometry), _i, _i, _pp], _i),
+    "ctgpu_helical_plan_views": ([_p, C.POINTER(_i)], _i),
+    "ctgpu_helical_plan_run": ([_p, _p, _i, _p, _i, _p, _i, C.c_longlong, _p, _p], _i),
+    "ctgpu_helical_plan_destroy": ([_p], None),
     "ctgpu_collect_projections_ellipsoids": ([_p, _p, _i, _d, _d, _p, _i, _p, _p], _i),
     "ctgpu_batch_create": ([C.POINTER(BatchProblem), _i, _i, _pp], _i),
     "ctgpu_batch_run": ([_p, _p], _i),

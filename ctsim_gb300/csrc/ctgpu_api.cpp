@@ -1318,6 +1318,120 @@ int ctgpu_halfscan_feather_equilinear(const ctgpu_geometry* g, float* d_data, in
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
+// Helical plan: Helical180LI (+ HalfScanFeather) at many interpolation views
+// of one data set, tables once, one gather launch per run.
+// ---------------------------------------------------------------------------
+struct ctgpu_helical_plan {
+  ctgpu_geometry g;
+  int nViewIn = 0, nOut = 0, flags = 0;
+  HelicalTap* d_interp = nullptr;
+  FeatherTap* d_feather = nullptr;
+  int* d_offsets = nullptr;
+  size_t d_offsets_cap = 0;
+  ~ctgpu_helical_plan() {
+    for (void* p : {(void*)d_interp, (void*)d_feather, (void*)d_offsets})
+      if (p) cudaFree(p);
+  }
+};
+
+extern "C" {
+
+int ctgpu_helical_plan_create(const ctgpu_geometry* g, int nViewIn, int flags,
+                              ctgpu_helical_plan** out) {
+  if (!g || !out) return fail(CTGPU_ERR_INVALID, "null argument");
+  const bool eql = (flags & CTGPU_HELICAL_EQUILINEAR) != 0;
+  int last, off;
+  int rc = helical_check(g, nViewIn, -1, &last, &off, eql);
+  if (rc) return rc;
+  std::unique_ptr<ctgpu_helical_plan> p(new ctgpu_helical_plan);
+  p->g = *g;
+  p->nViewIn = nViewIn;
+  p->nOut = last + 1;
+  p->flags = flags;
+  const int nDet = g->n_det;
+  // fan angle per detector, FP64 on the host (projections.cpp:247; the
+  // equilinear restatement maps the position through atan(pos / SDL))
+  std::vector<double> gam(nDet);
+  for (int id = 0; id < nDet; id++) {
+    const double pos = (id - (nDet - 1) / 2) * g->det_inc;
+    gam[id] = eql ? std::atan(pos / g->source_detector_length) : pos;
+  }
+  double* d_gam = nullptr;
+  const size_t nTab = (size_t)p->nOut * nDet;
+  CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&d_gam), sizeof(double) * nDet));
+  cudaError_t e = cudaMemcpy(d_gam, gam.data(), sizeof(double) * nDet, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->d_interp), sizeof(HelicalTap) * nTab);
+  if (e == cudaSuccess && (flags & CTGPU_HELICAL_FEATHER))
+    e = cudaMalloc(reinterpret_cast<void**>(&p->d_feather), sizeof(FeatherTap) * nTab);
+  if (e == cudaSuccess) {
+    HelicalLaunch L{};
+    L.nDet = nDet;
+    L.nViewIn = nViewIn;
+    L.nViewOut = p->nOut;
+    L.dbeta = g->rot_inc;
+    L.dgamma = g->det_inc;
+    L.fan = g->fan_beam_angle;
+    L.equilinear = eql ? 1 : 0;
+    L.sdl = g->source_detector_length;
+    e = launch_helical_tables(L, d_gam, p->d_interp, p->d_feather, nullptr);
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  cudaFree(d_gam);
+  CUDA_TRY(e);
+  *out = p.release();
+  return ok();
+}
+
+int ctgpu_helical_plan_views(const ctgpu_helical_plan* p, int* nOut) {
+  if (!p || !nOut) return fail(CTGPU_ERR_INVALID, "null argument");
+  *nOut = p->nOut;
+  return ok();
+}
+
+int ctgpu_helical_plan_run(ctgpu_helical_plan* p, const float* d_in, int inPitch,
+                           const int* interpViews, int nSlices, float* d_out, int outPitch,
+                           long long outSliceStride, double* h_angles, void* stream) {
+  if (!p || !d_in || !interpViews || !d_out || nSlices < 1) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (inPitch < p->g.n_det || outPitch < p->g.n_det ||
+      outSliceStride < (long long)outPitch * p->nOut)
+    return fail(CTGPU_ERR_INVALID, "pitch / slice stride too small");
+  const bool eql = (p->flags & CTGPU_HELICAL_EQUILINEAR) != 0;
+  std::vector<int> offs(nSlices);
+  for (int z = 0; z < nSlices; z++) {
+    int last, off;
+    int rc = helical_check(&p->g, p->nViewIn, interpViews[z], &last, &off, eql);
+    if (rc) return rc;
+    offs[z] = off;
+    if (h_angles)
+      for (int i = 0; i <= last; i++) h_angles[(size_t)z * p->nOut + i] = (i + off) * p->g.rot_inc;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(ensure_device(p->d_offsets, p->d_offsets_cap, (size_t)nSlices));
+  CUDA_TRY(cudaMemcpyAsync(p->d_offsets, offs.data(), sizeof(int) * nSlices,
+                           cudaMemcpyHostToDevice, st));
+  HelicalSlicesLaunch L{};
+  L.nDet = p->g.n_det;
+  L.nViewOut = p->nOut;
+  L.nSlices = nSlices;
+  L.inPitch = inPitch;
+  L.outPitch = outPitch;
+  L.in = d_in;
+  L.offsets = p->d_offsets;
+  L.interp = p->d_interp;
+  L.feather = p->d_feather;
+  L.sf = p->nOut * p->g.rot_inc / kPi;   // projections.cpp:434-437
+  L.out = d_out;
+  L.outSliceStride = (size_t)outSliceStride;
+  L.status = status_pointer();
+  CUDA_TRY(launch_helical_slices(L, st));
+  return ok();
+}
+
+void ctgpu_helical_plan_destroy(ctgpu_helical_plan* p) { delete p; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
 // Batched reconstruction of problems of uneven sizes.  Each problem keeps a
 // plan of its own (filter design, image grid, geometry); the set-up launches
 // of the problems (filter, interval rows, tile records) run as parallel

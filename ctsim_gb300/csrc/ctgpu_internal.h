@@ -114,6 +114,34 @@ struct HelicalLaunch {
 };
 constexpr unsigned int kStatusFeatherRange = 2u;
 
+// One output sample's 180LI terms: own ray (same view and detector) with
+// weight w0 when own != 0, complementary ray (view ivc >= 0, mirrored
+// detector) with weight wc; views counted from the slice's first input view.
+struct HelicalTap {
+  double w0, wc;
+  int own, ivc;
+};
+// HalfScanFeather of one output sample: the 180LI sample (v, d) times w;
+// bad: the reference's "Shouldn't be here" case
+struct FeatherTap {
+  double w;
+  int v, d, bad, pad;
+};
+struct HelicalSlicesLaunch {
+  int nDet, nViewOut, nSlices, inPitch, outPitch, pad;
+  const float* in;
+  const int* offsets;          // device, nSlices: first input view of each slice
+  const HelicalTap* interp;    // [nViewOut][nDet]
+  const FeatherTap* feather;   // [nViewOut][nDet] or null
+  double sf;                   // feathering's final scale nView * dbeta / pi
+  float* out;                  // [nSlices] x outSliceStride
+  size_t outSliceStride;
+  unsigned int* status;
+};
+cudaError_t launch_helical_tables(const HelicalLaunch& L, const double* gammaTab,
+                                  HelicalTap* interp, FeatherTap* feather, cudaStream_t s);
+cudaError_t launch_helical_slices(const HelicalSlicesLaunch& L, cudaStream_t s);
+
 // status bits written by kernels
 constexpr unsigned int kStatusTimeout = 1u;
 

@@ -142,3 +142,134 @@ cudaError_t launch_halfscan_feather(const HelicalLaunch& L, cudaStream_t s) {
 }
 
 }  // namespace ctgpu
+
+// ---------------------------------------------------------------------------
+// Many slices of one helical data set.  The 180LI weights and complementary
+// rays of an output sample, and the feathering that follows, depend only on
+// the geometry -- not on the interpolation view -- so they are tabulated once
+// (same FP64 expressions as the kernels above) and every run gathers all
+// slices in one launch: out = sf * (w_f * interp(vs, ds)) with
+// interp = own-ray term then complementary-ray term, in the reference's order
+// and FP32 roundings.
+// ---------------------------------------------------------------------------
+namespace ctgpu {
+
+__global__ void helical_tables_kernel(HelicalLaunch L, const double* __restrict__ gammaTab,
+                                      HelicalTap* __restrict__ interp,
+                                      FeatherTap* __restrict__ feather) {
+  const int vo = blockIdx.x;
+  const int nDet = L.nDet;
+  const double dbeta = L.dbeta, fan = L.fan, PI = kPi;
+  const int last = L.nViewOut - 1, lastAcq = 2 * last;
+  for (int dO = threadIdx.x; dO < nDet; dO += blockDim.x) {
+    HelicalTap t;
+    t.w0 = 0.0;
+    t.wc = 0.0;
+    t.own = 0;
+    t.ivc = -1;
+    {
+      double beta = vo * dbeta, gamma = gammaTab[dO], w;
+      if (beta < PI + fan && li_weight(beta, gamma, fan, &w)) {
+        t.own = 1;
+        t.w0 = w;
+      }
+    }
+    {
+      int id = nDet - 1 - dO;
+      double gamma = gammaTab[id];
+      int guess = (int)floor(vo - (2 * gamma - PI) / dbeta);
+      for (int iv = guess - 2; iv <= guess + 2; iv++) {
+        if (iv < 0 || iv > lastAcq) continue;
+        double beta = iv * dbeta;
+        if (beta < PI + fan) continue;
+        int nv = nearest_int(((iv * dbeta) + 2 * gamma - PI) / dbeta);
+        if (nv != vo) continue;
+        double w;
+        if (li_weight(beta, gamma, fan, &w)) {
+          t.ivc = iv;
+          t.wc = w;
+        }
+      }
+    }
+    interp[(size_t)vo * nDet + dO] = t;
+    if (feather) {
+      // halfscan_feather_kernel's choice for output sample (vo, dO)
+      FeatherTap f;
+      f.v = vo;
+      f.d = dO;
+      f.w = 1.0;
+      f.bad = 0;
+      double beta = vo * dbeta, gamma = gammaTab[dO];
+      if (beta >= PI - 2 * gamma) {
+        int iv1 = nearest_int(((vo * dbeta) + 2 * gamma - PI) / dbeta);
+        double w1;
+        if (!feather_w1(iv1 * dbeta, -gamma, fan, &w1)) { f.bad = 1; w1 = 0; }
+        f.w = 1 - w1;
+      } else {
+        int id2 = nDet - 1 - dO;
+        double gamma2 = gammaTab[id2];
+        int guess = (int)floor(vo + (PI - 2 * gamma2) / dbeta);
+        for (int iv2 = guess - 2; iv2 <= guess + 2; iv2++) {
+          if (iv2 < 0 || iv2 > last) continue;
+          double beta2 = iv2 * dbeta;
+          if (!(beta2 >= PI - 2 * gamma2)) continue;
+          int iv1 = nearest_int(((iv2 * dbeta) + 2 * gamma2 - PI) / dbeta);
+          if (iv1 != vo) continue;
+          double w1;
+          if (!feather_w1(vo * dbeta, -gamma2, fan, &w1)) { f.bad = 1; w1 = 0; }
+          f.v = iv2;
+          f.d = id2;
+          f.w = w1;
+        }
+      }
+      feather[(size_t)vo * nDet + dO] = f;
+    }
+  }
+}
+
+// 180LI value of output sample (vo, d) of the slice whose first input view is off
+__device__ __forceinline__ float helical_interp(const HelicalTap& t, const float* in, int off,
+                                                int pitch, int nDet, int vo, int d) {
+  float o = 0.f;
+  if (t.own) o = (float)((double)o + t.w0 * (double)in[(size_t)(vo + off) * pitch + d]);
+  if (t.ivc >= 0)
+    o = (float)((double)o + t.wc * (double)in[(size_t)(t.ivc + off) * pitch + (nDet - 1 - d)]);
+  return o;
+}
+
+// grid (output views, slices)
+__global__ void helical_slices_kernel(HelicalSlicesLaunch L) {
+  const int vo = blockIdx.x, z = blockIdx.y;
+  const int off = L.offsets[z];
+  float* out = L.out + (size_t)z * L.outSliceStride + (size_t)vo * L.outPitch;
+  for (int d = threadIdx.x; d < L.nDet; d += blockDim.x) {
+    float x;
+    if (L.feather) {
+      const FeatherTap f = L.feather[(size_t)vo * L.nDet + d];
+      if (f.bad) atomicOr(L.status, kStatusFeatherRange);
+      x = helical_interp(L.interp[(size_t)f.v * L.nDet + f.d], L.in, off, L.inPitch, L.nDet, f.v,
+                         f.d);
+      x = (float)((double)x * f.w);
+      x = (float)((double)x * L.sf);
+    } else {
+      x = helical_interp(L.interp[(size_t)vo * L.nDet + d], L.in, off, L.inPitch, L.nDet, vo, d);
+    }
+    out[d] = x;
+  }
+}
+
+cudaError_t launch_helical_tables(const HelicalLaunch& L, const double* gammaTab,
+                                  HelicalTap* interp, FeatherTap* feather, cudaStream_t s) {
+  helical_tables_kernel<<<L.nViewOut, 128, 0, s>>>(L, gammaTab, interp, feather);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_helical_slices(const HelicalSlicesLaunch& L, cudaStream_t s) {
+  if (L.nSlices <= 0) return cudaSuccess;
+  if (L.nSlices > 65535) return cudaErrorInvalidConfiguration;
+  dim3 grid(L.nViewOut, L.nSlices);
+  helical_slices_kernel<<<grid, 128, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+}  // namespace ctgpu

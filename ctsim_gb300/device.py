@@ -252,6 +252,40 @@ def halfscan_feather(geometry, sino, stream=None, equilinear=False):
     return sino
 
 
+class HelicalPlan:
+    """Helical180LI (+ HalfScanFeather) at many interpolation views of one data
+    set (ctgpu_helical_plan): tables once, all slices in one launch."""
+
+    def __init__(self, geometry, n_view_in, equilinear=False, feather=True):
+        flags = (1 if equilinear else 0) | (2 if feather else 0)
+        self._h = C.c_void_p()
+        check(lib().ctgpu_helical_plan_create(C.byref(geometry), n_view_in, flags,
+                                              C.byref(self._h)))
+        n = C.c_int()
+        check(lib().ctgpu_helical_plan_views(self._h, C.byref(n)))
+        self.n_view_out = n.value
+
+    def run(self, sino, interp_views, out=None, stream=None):
+        """sino [n_view_in, pitch] device tensor -> out [n_slices, n_view_out,
+        pitch]; returns (out, angles [n_slices, n_view_out])."""
+        torch = _torch()
+        iv = np.ascontiguousarray(interp_views, np.int32)
+        if out is None:
+            out = torch.empty((len(iv), self.n_view_out, sino.shape[1]), dtype=torch.float32,
+                              device=sino.device)
+        ang = np.zeros((len(iv), self.n_view_out), np.float64)
+        check(lib().ctgpu_helical_plan_run(self._h, _ptr(sino), sino.shape[1],
+                                           iv.ctypes.data_as(C.c_void_p), len(iv), _ptr(out),
+                                           out.shape[2], out.stride(0),
+                                           ang.ctypes.data_as(C.c_void_p), stream_handle(stream)))
+        return out, ang
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().ctgpu_helical_plan_destroy(self._h)
+            self._h = None
+
+
 def raysums_ellipsoids(scanner, ellipsoids, z0, dz, sino, stream=None):
     """Helical scan of a 3-D ellipsoid phantom (rows cx, cy, cz, a, b, c,
     rot_deg, atten): view v sees the cross-section at z0 + v dz.  Returns the

@@ -283,6 +283,26 @@ int ctgpu_helical180li_equilinear(const ctgpu_geometry* g, const float* d_in, in
                                   double* h_out_angles, int* n_view_out, void* stream);
 int ctgpu_halfscan_feather_equilinear(const ctgpu_geometry* g, float* d_data, int n_view,
                                       int pitch, void* stream);
+/* Helical180LI (+ HalfScanFeather) at many interpolation views of one helical
+ * data set of n_view_in views.  The FP64 weights and complementary rays of an
+ * output sample depend only on the geometry, so the plan tabulates them once;
+ * a run then interpolates every slice in one launch, with the same values as
+ * ctgpu_helical180li (+ ctgpu_halfscan_feather) slice by slice.  No reference
+ * counterpart as one call (pjHinterp does one interpolation view). */
+typedef struct ctgpu_helical_plan ctgpu_helical_plan;
+#define CTGPU_HELICAL_EQUILINEAR 1   /* the equilinear restatement above */
+#define CTGPU_HELICAL_FEATHER 2      /* follow each slice's 180LI by HalfScanFeather */
+int ctgpu_helical_plan_create(const ctgpu_geometry* g, int n_view_in, int flags,
+                              ctgpu_helical_plan** out);
+/* views of every output slice: (pi + fan) / rot_inc + 1 */
+int ctgpu_helical_plan_views(const ctgpu_helical_plan* p, int* n_view_out);
+/* d_in [n_view_in][in_pitch]; slice z interpolated at view interp_views[z]
+ * into d_out + z * out_slice_stride ([n_view_out][out_pitch]); its view angles
+ * to h_out_angles[z * n_view_out ..] when non-NULL */
+int ctgpu_helical_plan_run(ctgpu_helical_plan* p, const float* d_in, int in_pitch,
+                           const int* h_interp_views, int n_slices, float* d_out, int out_pitch,
+                           long long out_slice_stride, double* h_out_angles, void* stream);
+void ctgpu_helical_plan_destroy(ctgpu_helical_plan* p);
 
 /* ------------------------------------------------------------------------ */
 /* Allocation-free variant                                                   */
