@@ -97,6 +97,7 @@ SIGNATURES = {
     "ctgpu_helical_plan_views": ([_p, C.POINTER(_i)], _i),
     "ctgpu_helical_plan_run": ([_p, _p, _i, _p, _i, _p, _i, C.c_longlong, _p, _p], _i),
     "ctgpu_helical_plan_destroy": ([_p], None),
+    "ctgpu_raysum_ellipse_gradient": ([_p, _p, _p, _i, _p, _p], _i),
     "ctgpu_collect_projections_ellipsoids": ([_p, _p, _i, _d, _d, _p, _i, _p, _p], _i),
     "ctgpu_batch_create": ([C.POINTER(BatchProblem), _i, _i, _pp], _i),
     "ctgpu_batch_run": ([_p, _p], _i),

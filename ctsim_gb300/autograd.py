@@ -7,11 +7,18 @@ torch.autograd.Functions on the library's kernels.
 B is the parallel table backprojector with linear interpolation
 (libctsim/backprojectors.cpp:444-481) without its rotScale, B^T its exact
 transpose (same FP64 anchors and FP32 positions, weights (1-frac, frac)), and
-F the Toeplitz filter of the plan, which is symmetric for parallel beams
-(even filter kernels; no fan pre-weighting), so F^T = F.  Hence
+F the plan's filter, a Toeplitz operator (applied as an FFT convolution)
+that is symmetric for parallel beams (even filter kernels; no fan
+pre-weighting), so F^T = F.  Hence
     dP^T  = scale * B,      dFBP^T = F (rotScale * B^T).
 Views are recomputed in the backward pass, nothing per view is stored.
 Images are [nx, ny] float32 CUDA tensors, sinograms [n_view, pitch].
+
+    R(theta) = analytic ray-sums of a phantom of ellipses with parameters
+               theta [n, 6] = (cx, cy, u, v, rot_deg, atten) per ellipse
+               (ctgpu_collect_projections), any geometry;
+    dR^T g   = ctgpu_raysum_ellipse_gradient (chord-length derivatives,
+               outline-box pre-rejection held fixed).
 """
 import numpy as np
 import torch
@@ -90,3 +97,57 @@ def project(x, op):
 def fbp(sino, op):
     """Differentiable FBP(sino): [n_view, pitch] -> [nx, ny]."""
     return _FBP.apply(sino, op)
+
+
+class EllipseProjector:
+    """Analytic ray-sums of a phantom of ellipses as a function of their
+    parameters, with a fixed scanner (its geometry is not re-derived from the
+    parameters)."""
+
+    def __init__(self, scanner):
+        self.scanner = scanner
+        self.geometry = scanner.geometry()
+
+    def phantom(self, params):
+        from . import Phantom
+        p = Phantom()
+        for row in np.asarray(params, np.float64).reshape(-1, 6):
+            p.add_element("ellipse", *[float(x) for x in row])
+        return p
+
+    def project(self, params):
+        out = device.alloc_sinogram(self.geometry.n_view, self.geometry.n_det)
+        device.raysums(self.scanner, self.phantom(params), out)
+        return out
+
+    def gradient(self, params, g):
+        import ctypes as C
+        from ._lib import check, lib
+        p = self.phantom(params)
+        n = np.asarray(params).reshape(-1, 6).shape[0]
+        out = np.zeros((n, 6), np.float64)
+        gg = g.contiguous().float()
+        check(lib().ctgpu_raysum_ellipse_gradient(self.scanner._h, p._h, C.c_void_p(gg.data_ptr()),
+                                                  gg.shape[1], out.ctypes.data_as(C.c_void_p),
+                                                  None))
+        return out
+
+
+class _EllipseRaysums(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, params, op):
+        ctx.op = op
+        ctx.params = params.detach().cpu().numpy().astype(np.float64)
+        ctx.dtype, ctx.device = params.dtype, params.device
+        return op.project(ctx.params)
+
+    @staticmethod
+    def backward(ctx, g):
+        grad = ctx.op.gradient(ctx.params, g)
+        return torch.from_numpy(grad).to(dtype=ctx.dtype, device=ctx.device), None
+
+
+def ellipse_raysums(params, op):
+    """Sinogram [n_view, pitch] of the ellipses `params` [n, 6] (cx, cy, u, v,
+    rot_deg, atten); differentiable in params."""
+    return _EllipseRaysums.apply(params, op)

@@ -765,6 +765,50 @@ int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ell, in
   return ok();
 }
 
+int ctgpu_raysum_ellipse_gradient(ctgpu_scanner* s, const ctgpu_phantom* p,
+                                  const float* d_gsino, int pitch, double* h_grad, void* stream) {
+  if (!s || !p || !d_gsino || !h_grad) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (pitch < s->nDet) return fail(CTGPU_ERR_INVALID, "sinogram pitch smaller than nDet");
+  const int n = (int)p->elems.size();
+  for (const PElem& e : p->elems)
+    if (e.type != kEllipse)
+      return fail(CTGPU_ERR_UNSUPPORTED, "parameter gradients are defined for ellipse elements");
+  if (p->unitPulse) return fail(CTGPU_ERR_UNSUPPORTED, "unit-pulse phantom");
+  cudaStream_t st = (cudaStream_t)stream;
+  scanner_views(s, 0, s->nView, s->offsetView);
+  CUDA_TRY(const_cast<ctgpu_phantom*>(p)->upload(st));
+  CUDA_TRY(upload_ray_views(s, s->nView, st));
+  double* d_grad = nullptr;
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d_grad), sizeof(double) * 6 * (n > 0 ? n : 1), st));
+  RaysumLaunch L{};
+  L.geometry = s->geometry;
+  L.nDet = s->nDet;
+  L.nSample = s->nSample;
+  L.nElem = n;
+  L.nViews = s->nView;
+  L.pitch = pitch;
+  L.centerDetectorLength = s->centerDetectorLength;
+  L.elems = p->d_elems;
+  L.views = s->d_views;
+  L.sdirs = s->d_sdirs;
+  std::vector<double> g(6 * (size_t)(n > 0 ? n : 1), 0.0);
+  cudaError_t e = cudaMemsetAsync(d_grad, 0, sizeof(double) * g.size(), st);
+  if (e == cudaSuccess) e = launch_raysum_ellipse_grad(L, d_gsino, d_grad, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g.data(), d_grad, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(d_grad, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaErrorInvalidValue) return fail(CTGPU_ERR_UNSUPPORTED, "too many detectors x rays for one CTA");
+  CUDA_TRY(e);
+  // list index k holds the element added (n-1-k)th; rotation per degree
+  for (int k = 0; k < n; k++) {
+    double* o = h_grad + 6 * (size_t)(n - 1 - k);
+    for (int j = 0; j < 6; j++) o[j] = g[6 * (size_t)k + j];
+    o[4] *= kPi / 180.0;
+  }
+  return ok();
+}
+
 int ctgpu_collect_projections_host(ctgpu_scanner* s, const ctgpu_phantom* p, int startView,
                                    int nViews, int offsetView, int storageOffset, float* h_sino,
                                    double* h_angles) {

@@ -159,6 +159,10 @@ cudaError_t launch_raysum(const RaysumLaunch& L, cudaStream_t s);
 // is the ellipse cut at z0 + v dz, scaled about its centre, or absent.
 cudaError_t launch_ellipsoid_sections(const PElem* base, const double2* zc, int n, int nViews,
                                       double z0, double dz, PElem* out, cudaStream_t s);
+// d(sum_{v,d} gsino[v][d] sino[v][d]) / d(cx, cy, u, v, theta, atten) of every
+// element (ellipses) into grad[6 * nElem] (FP64, accumulated: zero it first)
+cudaError_t launch_raysum_ellipse_grad(const RaysumLaunch& L, const float* gsino, double* grad,
+                                       cudaStream_t s);
 // scratch of launch_raysum: one record per (phantom, view, element, ray sample)
 size_t raysum_record_bytes(const RaysumLaunch& L, int totalElems);
 cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int rowOffset,

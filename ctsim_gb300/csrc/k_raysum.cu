@@ -497,3 +497,137 @@ cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int 
 }
 
 }  // namespace ctgpu
+
+// ---------------------------------------------------------------------------
+// Gradient of the ray-sums with respect to the ellipses' parameters (no
+// reference counterpart).  For a ray with unit direction r through the point
+// S, an ellipse with centre W, semi-axes u, v, rotation theta and attenuation
+// a has signed distance rho = cross(r, W - S) and, with (ra, rb) = r in the
+// ellipse frame, Q = v^2 ra^2 + u^2 rb^2, hc^2 = Q - rho^2, the chord
+//   c = 2 u v hc / Q   (hc^2 > 0; 0 otherwise)
+// whose partial derivatives are
+//   dc/drho = -2 u v rho / (Q hc)              drho/dW = (-ry, rx)
+//   dc/dQ   = u v (2 rho^2 - Q) / (hc Q^2)     dQ/du = 2 u rb^2, dQ/dv = 2 v ra^2,
+//   dc/du  |= 2 v hc / Q,  dc/dv |= 2 u hc / Q  dQ/dtheta = 2 ra rb (v^2 - u^2)
+// A ray counts for an ellipse as in the forward model: hc^2 > 0 and accepted
+// by the reference's outline-box clip (held fixed in the derivative).  The
+// derivative grows like 1/hc at tangency, so the terms are formed in FP64
+// (FP32's rounding of hc^2 would dominate there); the detector value is the
+// mean over its ray samples.  One CTA per view: the rays are staged in
+// shared memory, then per ellipse each thread accumulates its rays' six
+// terms, warps reduce, and the CTA's totals go to FP64 global accumulators.
+// ---------------------------------------------------------------------------
+namespace ctgpu {
+
+struct GradRay { double rx, ry, sx, sy, xd, yd, g; };
+
+template <int GEOM>
+__global__ void __launch_bounds__(128) raysum_ellipse_grad_kernel(RaysumLaunch L,
+                                                                  const float* __restrict__ gsino,
+                                                                  double* __restrict__ grad) {
+  extern __shared__ __align__(16) unsigned char smg[];
+  GradRay* rays = reinterpret_cast<GradRay*>(smg);
+  const int view = blockIdx.x;
+  const RayView& g = L.views[view];
+  const int nS = L.nSample, nRay = L.nDet * nS;
+  const float* gv = gsino + (size_t)(L.rowOffset + view) * L.pitch;
+  for (int t = threadIdx.x; t < nRay; t += blockDim.x) {
+    const int d = t / nS;
+    GradRay R;
+    double sx = g.S0x, sy = g.S0y, px, py;
+    if (GEOM == kEquiangular) {
+      double sa, ca;
+      sincos(g.alpha0 + (double)t * g.delta, &sa, &ca);
+      px = L.centerDetectorLength * ca;
+      py = L.centerDetectorLength * sa;
+    } else {
+      if (GEOM == kParallel) {
+        sx += d * g.dSx;
+        sy += d * g.dSy;
+      }
+      px = g.D0x + (double)t * g.dDx;
+      py = g.D0y + (double)t * g.dDy;
+    }
+    double dx = px - sx, dy = py - sy;
+    const double n = 1.0 / sqrt(dx * dx + dy * dy);
+    R.rx = dx * n;
+    R.ry = dy * n;
+    R.sx = sx;
+    R.sy = sy;
+    R.xd = px;
+    R.yd = py;
+    R.g = (double)gv[d] / nS;
+    rays[t] = R;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (int k = 0; k < L.nElem; k++) {
+    const PElem& pe = L.elems[k];
+    const double cx = pe.cx, cy = pe.cy, u = pe.u, v = pe.v;
+    const double ct = pe.cosr, st = pe.sinr, at = pe.atten;
+    const double bcx = 0.5 * (pe.bx0 + pe.bx1), bcy = 0.5 * (pe.by0 + pe.by1);
+    const double rin = fmin(pe.bx1 - pe.bx0, pe.by1 - pe.by0) * 0.5 * (1.0 - 1e-9);
+    const double lim[4] = {pe.bx0, pe.by0, pe.bx1, pe.by1};
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int t = threadIdx.x; t < nRay; t += blockDim.x) {
+      const GradRay R = rays[t];
+      const double rho = R.rx * (cy - R.sy) - R.ry * (cx - R.sx);
+      const double ra = R.rx * ct + R.ry * st, rb = -R.rx * st + R.ry * ct;
+      const double Q = v * v * ra * ra + u * u * rb * rb;
+      const double h2 = Q - rho * rho;
+      if (!(h2 > 0.0)) continue;
+      // the forward model's outline-box acceptance: certain inside the box's
+      // inscribed circle, else the reference's clip on the ray's end points
+      const double rbox = R.rx * (bcy - R.sy) - R.ry * (bcx - R.sx);
+      if (!(fabs(rbox) < rin) && !clip_rect_fp64(R.xd, R.yd, R.sx, R.sy, lim)) continue;
+      const double hc = sqrt(h2);
+      const double iQ = 1.0 / Q;
+      const double c = 2.0 * u * v * hc * iQ;
+      const double dcdrho = -2.0 * u * v * rho * iQ / hc;
+      const double dcdQ = u * v * (2.0 * rho * rho - Q) * iQ * iQ / hc;
+      const double ga = R.g * at;
+      acc[0] += ga * dcdrho * -R.ry;                                   // cx
+      acc[1] += ga * dcdrho * R.rx;                                    // cy
+      acc[2] += ga * (2.0 * v * hc * iQ + dcdQ * 2.0 * u * rb * rb);   // u
+      acc[3] += ga * (2.0 * u * hc * iQ + dcdQ * 2.0 * v * ra * ra);   // v
+      acc[4] += ga * dcdQ * 2.0 * ra * rb * (v * v - u * u);           // theta (radians)
+      acc[5] += R.g * c;                                               // attenuation
+    }
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+      double a = acc[j];
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0) atomicAdd(&grad[6 * k + j], a);
+    }
+  }
+}
+
+cudaError_t launch_raysum_ellipse_grad(const RaysumLaunch& L, const float* gsino, double* grad,
+                                       cudaStream_t s) {
+  if (L.nViews <= 0 || L.nElem <= 0) return cudaSuccess;
+  const size_t smem = sizeof(GradRay) * (size_t)L.nDet * L.nSample;
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  switch (L.geometry) {
+    case kParallel:
+      if (smem > 48 * 1024)
+        cudaFuncSetAttribute(raysum_ellipse_grad_kernel<kParallel>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      raysum_ellipse_grad_kernel<kParallel><<<L.nViews, 128, smem, s>>>(L, gsino, grad);
+      break;
+    case kEquilinear:
+      if (smem > 48 * 1024)
+        cudaFuncSetAttribute(raysum_ellipse_grad_kernel<kEquilinear>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      raysum_ellipse_grad_kernel<kEquilinear><<<L.nViews, 128, smem, s>>>(L, gsino, grad);
+      break;
+    default:
+      if (smem > 48 * 1024)
+        cudaFuncSetAttribute(raysum_ellipse_grad_kernel<kEquiangular>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      raysum_ellipse_grad_kernel<kEquiangular><<<L.nViews, 128, smem, s>>>(L, gsino, grad);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace ctgpu

@@ -139,6 +139,16 @@ int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ellipso
                                          int n_ellipsoids, double z0, double dz_per_view,
                                          float* d_sino, int sino_pitch, double* h_view_angles,
                                          void* stream);
+/* Gradient of the ray-sums of all n_view views with respect to the phantom's
+ * ellipse parameters: h_grad[6 j + m] = sum over views v and detectors d of
+ * d_grad_sino[v][d] * d sino[v][d] / d param_m of the j-th element added,
+ * params (cx, cy, u, v, rot_deg, atten) as ctgpu_phantom_add_element.  Every
+ * element must be an ellipse; the outline-box pre-rejection is held fixed
+ * (it changes no chord but at tangency).  Synchronous.  No reference
+ * counterpart (CTSim computes no derivatives). */
+int ctgpu_raysum_ellipse_gradient(ctgpu_scanner* s, const ctgpu_phantom* p,
+                                  const float* d_grad_sino, int sino_pitch, double* h_grad,
+                                  void* stream);
 void ctgpu_scanner_destroy(ctgpu_scanner* s);
 
 /* ------------------------------------------------------------------------ */

@@ -573,6 +573,101 @@ void ora_collect_projections(const ora_scanner* s, const ora_phantom* p, int iSt
   free(vp);
 }
 
+/* Gradient of sum_{v,d} gsino[v][d] sino[v][d] with respect to the ellipse
+ * parameters (cx, cy, u, v, rot radians, atten) of every element (list
+ * order), FP64.  No reference counterpart: the derivative of the chord
+ * c = 2 u v sqrt(Q - rho^2) / Q, Q = v^2 ra^2 + u^2 rb^2, of each ray that
+ * projectSingleView (scanner.cpp:445-533) traces and the element's outline
+ * box accepts (scanner.cpp:611-656 with phantom.cpp:830-850), the box held
+ * fixed.  Views as ora_collect_projections over all views. */
+static void ray_grad(const ora_phantom* p, double xd, double yd, double xs, double ys, double w,
+                     double* grad) {
+  double dx = xd - xs, dy = yd - ys, n = 1.0 / sqrt(dx * dx + dy * dy);
+  double rx = dx * n, ry = dy * n;
+  for (int k = 0; k < p->n; k++) {
+    const ora_pelem* e = &p->e[k];
+    if (e->type != ORA_PELEM_ELLIPSE) continue;
+    double ct = cos(e->rot), st = sin(e->rot), u = e->u, v = e->v;
+    double rho = rx * (e->cy - ys) - ry * (e->cx - xs);
+    double ra = rx * ct + ry * st, rb = -rx * st + ry * ct;
+    double Q = v * v * ra * ra + u * u * rb * rb, h2 = Q - rho * rho;
+    if (!(h2 > 0.0)) continue;
+    double lim[4] = {e->xmin, e->ymin, e->xmax, e->ymax};
+    double x1 = xd, y1 = yd, x2 = xs, y2 = ys;
+    if (!clip_rect(&x1, &y1, &x2, &y2, lim)) continue;
+    double hc = sqrt(h2), iQ = 1.0 / Q, c = 2.0 * u * v * hc * iQ;
+    double dcdrho = -2.0 * u * v * rho * iQ / hc;
+    double dcdQ = u * v * (2.0 * rho * rho - Q) * iQ * iQ / hc;
+    double ga = w * e->atten, *g = grad + 6 * k;
+    g[0] += ga * dcdrho * -ry;
+    g[1] += ga * dcdrho * rx;
+    g[2] += ga * (2.0 * v * hc * iQ + dcdQ * 2.0 * u * rb * rb);
+    g[3] += ga * (2.0 * u * hc * iQ + dcdQ * 2.0 * v * ra * ra);
+    g[4] += ga * dcdQ * 2.0 * ra * rb * (v * v - u * u);
+    g[5] += w * c;
+  }
+}
+
+void ora_ellipse_gradient(const ora_scanner* s, const ora_phantom* p, const double* gsino,
+                          double* grad) {
+  int nv = s->nView, nDet = s->nDet, nSample = s->nSample;
+  for (int i = 0; i < 6 * p->n; i++) grad[i] = 0;
+  mtx2 m0, t;
+  m_xlat(m0, -s->xCenter, -s->yCenter);
+  m_rot(t, s->offsetView * s->rotInc); m_mul(m0, t, m0);
+  m_xlat(t, s->xCenter, s->yCenter); m_mul(m0, t, m0);
+  double xd1 = 0, yd1 = 0, xd2 = 0, yd2 = 0;
+  if (s->geometry != ORA_GEOM_EQUIANGULAR) {
+    xd1 = s->xd1; yd1 = s->yd1; xd2 = s->xd2; yd2 = s->yd2;
+    m_apply((const double(*)[3])m0, &xd1, &yd1);
+    m_apply((const double(*)[3])m0, &xd2, &yd2);
+  }
+  double xs1 = s->xs1, ys1 = s->ys1, xs2 = s->xs2, ys2 = s->ys2;
+  m_apply((const double(*)[3])m0, &xs1, &ys1);
+  m_apply((const double(*)[3])m0, &xs2, &ys2);
+  double ang = s->offsetView * s->rotInc;
+  for (int vi = 0; vi < nv; vi++, ang += s->rotInc) {
+    /* the rays of projectSingleView for this view */
+    double sdx = (xs2 - xs1) / nDet, sdy = (ys2 - ys1) / nDet;
+    double xs_maj = xs1 + (sdx / 2), ys_maj = ys1 + (sdy / 2);
+    double ddx = 0, ddy = 0, ddx2 = 0, ddy2 = 0, xd_maj = 0, yd_maj = 0;
+    double angInc = 0, angSampleInc = 0, angMajor = 0;
+    if (s->geometry == ORA_GEOM_EQUIANGULAR) {
+      angInc = s->angularDetInc;
+      angSampleInc = angInc / nSample;
+      angMajor = ang + 3 * O_HALFPI - (s->angularDetLen / 2) + angSampleInc / 2;
+    } else {
+      ddx = (xd2 - xd1) / nDet; ddy = (yd2 - yd1) / nDet;
+      ddx2 = ddx / nSample; ddy2 = ddy / nSample;
+      xd_maj = xd1 + ddx2 / 2; yd_maj = yd1 + ddy2 / 2;
+    }
+    for (int d = 0; d < nDet; d++) {
+      double xs = xs_maj, ys = ys_maj, xd = 0, yd = 0, a = 0;
+      if (s->geometry == ORA_GEOM_EQUIANGULAR) a = angMajor;
+      else { xd = xd_maj; yd = yd_maj; }
+      double w = gsino[(size_t)vi * nDet + d] / nSample;
+      for (int i = 0; i < nSample; i++) {
+        if (s->geometry == ORA_GEOM_EQUIANGULAR) {
+          xd = s->centerDetectorLength * cos(a);
+          yd = s->centerDetectorLength * sin(a);
+        }
+        ray_grad(p, xd, yd, xs, ys, w, grad);
+        if (s->geometry == ORA_GEOM_EQUIANGULAR) a += angSampleInc;
+        else { xd += ddx2; yd += ddy2; }
+      }
+      xs_maj += sdx; ys_maj += sdy;
+      if (s->geometry == ORA_GEOM_EQUIANGULAR) angMajor += angInc;
+      else { xd_maj += ddx; yd_maj += ddy; }
+    }
+    m_apply(s->incmtx, &xs1, &ys1);
+    m_apply(s->incmtx, &xs2, &ys2);
+    if (s->geometry != ORA_GEOM_EQUIANGULAR) {
+      m_apply(s->incmtx, &xd1, &yd1);
+      m_apply(s->incmtx, &xd2, &yd2);
+    }
+  }
+}
+
 /* Helical scan of a 3-D ellipsoid phantom: a restatement with no reference
  * counterpart (CTSim's phantoms are 2-D).  View v of the scanner (positions
  * as collectProjections over all views, scanner.cpp:295-419) sees the

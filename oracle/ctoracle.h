@@ -85,6 +85,10 @@ void ora_collect_projections(const ora_scanner* s, const ora_phantom* p, int iSt
                              int iNumViews, int iOffsetView, int iStorageOffset, double* sino,
                              double* viewAngles, int nThreads);
 double ora_raysum(const ora_phantom* p, double x1, double y1, double x2, double y2);
+/* d(sum gsino * sino)/d(cx, cy, u, v, rot radians, atten) of the ellipses
+ * (list order), FP64; gsino [nView][nDet]; grad [6 * n] */
+void ora_ellipse_gradient(const ora_scanner* s, const ora_phantom* p, const double* gsino,
+                          double* grad);
 /* helical scan of a 3-D ellipsoid phantom (restatement only); ell[8k..8k+7] =
  * cx, cy, cz, a, b, c, rot_deg, atten; view v sees z = z0 + v dz */
 void ora_collect_ellipsoids(const ora_scanner* s, const double* ell, int n, double z0, double dz,

@@ -90,6 +90,7 @@ def lib():
         _LIB.ora_helical180li_ex.argtypes = [C.POINTER(Geom), p, i, i, p, p, C.POINTER(C.c_int), i]
         _LIB.ora_halfscan_feather_ex.argtypes = [C.POINTER(Geom), p, i, i]
         _LIB.ora_collect_ellipsoids.argtypes = [C.POINTER(_Scanner), p, i, d, d, p, p, i]
+        _LIB.ora_ellipse_gradient.argtypes = [C.POINTER(_Scanner), C.POINTER(_Phantom), p, p]
         _LIB.ora_phantom_to_image.argtypes = [C.POINTER(_Phantom), i, i, d, i, p, p, i]
         _LIB.ora_project_image.argtypes = [C.POINTER(Geom), p, i, i, p, i, p, i]
         _LIB.ora_frequency_response.argtypes = [i, d, d, d]
@@ -190,6 +191,19 @@ class Scanner:
                                       self.offset_view, start, _ptr(sino), _ptr(ang),
                                       nthreads or nthreads_default())
         return sino, ang
+
+
+def ellipse_gradient(scanner, gsino):
+    """FP64 d(sum gsino * sino)/d(cx, cy, u, v, rot_deg, atten) of the scanner's
+    phantom's ellipses, in the order they were added ([n, 6])."""
+    s = scanner._s
+    p = scanner.phantom._p
+    g = np.ascontiguousarray(gsino, np.float64)
+    out = np.zeros(6 * p.n, np.float64)
+    lib().ora_ellipse_gradient(C.byref(s), C.byref(p), _ptr(g), _ptr(out))
+    out = out.reshape(p.n, 6)[::-1].copy()   # list order is last added first
+    out[:, 4] *= np.pi / 180.0
+    return out
 
 
 def collect_ellipsoids(scanner, ellipsoids, z0, dz, nthreads=None):

@@ -112,3 +112,47 @@ def test_fbp_loss_gradient(setup, oracle):
     fd = (L(s.detach() + h * d) - L(s.detach() - h * d)) / (2 * h)
     an = float((gs.double() * d.double()).sum())
     assert abs(fd - an) <= 1e-3 * abs(an) + 1e-6, (fd, an)
+
+
+@pytest.mark.parametrize("geo", ["parallel", "equiangular", "equilinear"])
+def test_ellipse_parameter_gradient(setup, oracle, geo):
+    """d/d(cx, cy, u, v, rot, atten) of sum(G * R(theta)) for 12 ellipses through
+    the autograd Function: the adjoint kernel against the oracle's FP64
+    gradient of the same rays (itself pinned to FP64 central differences in
+    tests/test_oracle_gradient.py), per entry to 1e-6 of the larger of the
+    entry and 1% of its column's largest.  Central differences with h = 1e-3
+    do not apply here: a ray-sum is not differentiable at the tangent rays
+    (the chord has a square-root edge), so a step of that size measures the
+    kinks, not the derivative."""
+    torch, cg, autograd, op, g, ang, _ = setup
+    from ctsim_gb300 import device, phantoms
+    rows = phantoms.random_ellipses(seed=21, n=12)
+    theta = np.array([r[1:] for r in rows], np.float64)
+    nd, nv = 257, 180
+    sc = cg.Scanner(phantoms.make_phantom(rows), geo, nd, nv)
+    eop = autograd.EllipseProjector(sc)
+    G = np.random.default_rng(2).standard_normal((nv, nd)).astype(np.float32)
+    Gd = torch.zeros((nv, device.pitch_for(nd)), device="cuda")
+    Gd[:, :nd] = torch.from_numpy(G).cuda()
+    t = torch.tensor(theta, requires_grad=True)
+    sino = autograd.ellipse_raysums(t, eop)
+    loss = (sino * Gd).sum()
+    loss.backward()
+    grad = t.grad.numpy()
+    osc = oracle.Scanner(oracle.Phantom(elements=rows), geo, nd, nv)
+    ref = oracle.ellipse_gradient(osc, G.astype(np.float64))
+    scale = np.abs(ref).max(axis=0)
+    err = np.abs(grad - ref) / np.maximum(np.abs(ref), 1e-2 * scale)
+    print("%s ellipse-parameter gradient vs FP64 reference: max rel %.3g" % (geo, err.max()))
+    assert err.max() < 1e-6, err.max()
+    # the loss ||R(theta) - b||^2 of a perturbed phantom: its gradient is the
+    # same adjoint applied to 2 (R - b)
+    b = autograd.ellipse_raysums(torch.tensor(theta * 1.01), eop).detach()
+    t2 = torch.tensor(theta, requires_grad=True)
+    r = autograd.ellipse_raysums(t2, eop)
+    ((r - b) ** 2).sum().backward()
+    resid = (2 * (r - b)).detach()[:, :nd].cpu().numpy().astype(np.float64)
+    ref2 = oracle.ellipse_gradient(osc, resid)
+    s2 = np.abs(ref2).max(axis=0)
+    e2 = np.abs(t2.grad.numpy() - ref2) / np.maximum(np.abs(ref2), 1e-2 * s2)
+    assert e2.max() < 1e-6, e2.max()
