@@ -178,6 +178,27 @@ class Projections(fileio.ProjectionFile):
 
     HalfScanFeather = halfscan_feather
 
+    def interpolate_to_parallel(self):
+        """Projections::interpolateToParallel: a new parallel-beam Projections
+        (self for parallel data)."""
+        from . import device
+        import copy
+        if int(self.geometry) == 0:
+            return self
+        out, g, ang = device.interpolate_to_parallel(self.ctgpu_geometry(),
+                                                     device._to_device(self.data), self.angles)
+        sync()
+        q = copy.copy(self)
+        q.geometry, q.rotStart, q.rotInc = 0, g.rot_start, g.rot_inc
+        q.detStart, q.detInc = g.det_start, g.det_inc
+        q.angles = ang
+        q.data = out[:, :self.nDet].cpu().numpy()
+        q.calcTime = 0.0
+        q.remark = (self.remark or "") + "; Interpolate to Parallel"
+        return q
+
+    interpolateToParallel = interpolate_to_parallel
+
 
 class ImageFile(fileio.ImageFileData):
     """nx x ny FP32 image, column-major v[ix][iy] (F32Image)."""

@@ -93,6 +93,8 @@ SIGNATURES = {
     "ctgpu_helical180li_equilinear": ([C.POINTER(Geometry), _p, _i, _i, _p, _i, _p, C.POINTER(_i),
                                        _p], _i),
     "ctgpu_halfscan_feather_equilinear": ([C.POINTER(Geometry), _p, _i, _i, _p], _i),
+    "ctgpu_interpolate_to_parallel": ([C.POINTER(Geometry), _p, _i, _p, _p, _i,
+                                       C.POINTER(Geometry), _p, _p], _i),
     "ctgpu_helical_plan_create": ([C.POINTER(Geometry), _i, _i, _pp], _i),
     "ctgpu_helical_plan_views": ([_p, C.POINTER(_i)], _i),
     "ctgpu_helical_plan_run": ([_p, _p, _i, _p, _i, _p, _i, C.c_longlong, _p, _p], _i),

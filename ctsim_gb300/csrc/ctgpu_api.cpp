@@ -1361,6 +1361,99 @@ int ctgpu_halfscan_feather_equilinear(const ctgpu_geometry* g, float* d_data, in
 
 }  // extern "C"
 
+extern "C" {
+
+// Projections::interpolateToParallel (projections.cpp:1250-1328): the host
+// builds the reference's FP64 tables (fan angle and t = FL sin(gamma) of each
+// detector, accumulated output angles and positions), the device sorts and
+// interpolates (k_rebin.cu).
+int ctgpu_interpolate_to_parallel(const ctgpu_geometry* g, const float* d_sino, int pitch,
+                                  const double* h_angles, float* d_out, int outPitch,
+                                  ctgpu_geometry* gOut, double* h_outAngles, void* stream) {
+  if (!g || !d_sino || !h_angles || !d_out || !gOut || !h_outAngles)
+    return fail(CTGPU_ERR_INVALID, "null argument");
+  const int nDet = g->n_det, nView = g->n_view;
+  if (nDet < 1 || nView < 1 || pitch < nDet || outPitch < nDet)
+    return fail(CTGPU_ERR_INVALID, "bad sizes");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g->geometry == kParallel) {   // returns the projections themselves
+    *gOut = *g;
+    for (int v = 0; v < nView; v++) h_outAngles[v] = h_angles[v];
+    CUDA_TRY(cudaMemcpy2DAsync(d_out, sizeof(float) * outPitch, d_sino, sizeof(float) * pitch,
+                               sizeof(float) * nDet, nView, cudaMemcpyDeviceToDevice, st));
+    return ok();
+  }
+  if (g->geometry != kEquiangular && g->geometry != kEquilinear)
+    return fail(CTGPU_ERR_INVALID, "Invalid geometry");
+  if (rebin_sort_bytes(nView) > 200 * 1024)
+    return fail(CTGPU_ERR_UNSUPPORTED, "too many views to sort one detector's rays in shared memory");
+  ctgpu_geometry o = *g;
+  o.geometry = kParallel;
+  o.rot_start = 0;
+  o.rot_inc = 2 * kPi / nView;
+  o.det_start = -g->view_diameter / 2;
+  o.det_inc = g->view_diameter / nDet;
+  if (nDet % 2 == 0) o.det_inc = g->view_diameter / (nDet - 1);
+  std::vector<double> gam(nDet), t(nDet), tSorted(nDet), thOut(nView), posOut(nDet);
+  std::vector<int> order(nDet), group(nDet);
+  double dp = g->det_start;
+  for (int d = 0; d < nDet; d++, dp += g->det_inc) {
+    gam[d] = g->geometry == kEquilinear ? std::atan(dp / g->source_detector_length) : dp;
+    t[d] = g->focal_length * std::sin(gam[d]);
+    order[d] = d;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return t[a] < t[b]; });
+  for (int r = 0; r < nDet; r++) {
+    group[order[r]] = r;
+    tSorted[r] = t[order[r]];
+  }
+  double a = g->rot_start;
+  for (int v = 0; v < nView; v++, a += o.rot_inc) thOut[v] = a;
+  double p = o.det_start;
+  for (int d = 0; d < nDet; d++, p += o.det_inc) posOut[d] = p;
+  // one device block: angles, gam, thetaOut, tSorted, posOut (doubles), group (ints), tmp
+  const size_t nd = (size_t)nView * 2 + (size_t)nDet * 3;
+  const size_t bytes = sizeof(double) * nd + sizeof(int) * nDet + 16 + sizeof(float) * (size_t)nView * nDet;
+  unsigned char* blk = nullptr;
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&blk), bytes, st));
+  double* dd = reinterpret_cast<double*>(blk);
+  std::vector<double> host;
+  host.reserve(nd);
+  host.insert(host.end(), h_angles, h_angles + nView);
+  host.insert(host.end(), gam.begin(), gam.end());
+  host.insert(host.end(), thOut.begin(), thOut.end());
+  host.insert(host.end(), tSorted.begin(), tSorted.end());
+  host.insert(host.end(), posOut.begin(), posOut.end());
+  int* di = reinterpret_cast<int*>(dd + nd);
+  float* tmp = reinterpret_cast<float*>(blk + ((sizeof(double) * nd + sizeof(int) * nDet + 15) & ~(size_t)15));
+  cudaError_t e = cudaMemcpyAsync(dd, host.data(), sizeof(double) * nd, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(di, group.data(), sizeof(int) * nDet, cudaMemcpyHostToDevice, st);
+  RebinLaunch L{};
+  L.nDet = nDet;
+  L.nView = nView;
+  L.pitch = pitch;
+  L.outPitch = outPitch;
+  L.in = d_sino;
+  L.angles = dd;
+  L.gam = dd + nView;
+  L.thetaOut = dd + nView + nDet;
+  L.tSorted = dd + 2 * nView + nDet;
+  L.posOut = dd + 2 * nView + 2 * nDet;
+  L.group = di;
+  L.tmp = tmp;
+  L.out = d_out;
+  if (e == cudaSuccess) e = launch_rebin(L, st);
+  cudaFreeAsync(blk, st);
+  // the host tables are staged by the pageable copies before they return
+  CUDA_TRY(e);
+  *gOut = o;
+  for (int v = 0; v < nView; v++) h_outAngles[v] = thOut[v];
+  return ok();
+}
+
+}  // extern "C"
+
 // ---------------------------------------------------------------------------
 // Helical plan: Helical180LI (+ HalfScanFeather) at many interpolation views
 // of one data set, tables once, one gather launch per run.

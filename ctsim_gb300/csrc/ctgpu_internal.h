@@ -138,6 +138,22 @@ struct HelicalSlicesLaunch {
   size_t outSliceStride;
   unsigned int* status;
 };
+// Projections::interpolateToParallel on the device (k_rebin.cu)
+struct RebinLaunch {
+  int nDet, nView, pitch, outPitch, sortN, pad;
+  const float* in;          // [nView][pitch] fan-beam
+  const double* angles;     // nView view angles
+  const double* gam;        // nDet: fan angle of each detector
+  const int* group;         // nDet: rank of the detector's t = FL sin(gamma)
+  const double* thetaOut;   // nView output view angles
+  const double* tSorted;    // nDet: t of each rank
+  const double* posOut;     // nDet output detector positions
+  float* tmp;               // [nView][nDet]
+  float* out;               // [nView][outPitch]
+};
+cudaError_t launch_rebin(RebinLaunch L, cudaStream_t s);
+size_t rebin_sort_bytes(int nView);
+
 cudaError_t launch_helical_tables(const HelicalLaunch& L, const double* gammaTab,
                                   HelicalTap* interp, FeatherTap* feather, cudaStream_t s);
 cudaError_t launch_helical_slices(const HelicalSlicesLaunch& L, cudaStream_t s);

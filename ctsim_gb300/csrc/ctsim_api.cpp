@@ -339,6 +339,36 @@ int Projections::HalfScanFeather() {   // projections.cpp:369-439
   return 0;
 }
 
+Projections* Projections::interpolateToParallel() const {   // projections.cpp:1250-1328
+  if (m_g.geometry == CTGPU_GEOMETRY_PARALLEL) return const_cast<Projections*>(this);
+  Projections* q = new Projections(m_g.n_view, m_g.n_det);
+  size_t inBytes = sizeof(float) * (size_t)m_g.n_view * m_pitch;
+  size_t outBytes = sizeof(float) * (size_t)m_g.n_view * q->m_pitch;
+  float *dIn = nullptr, *dOut = nullptr;
+  std::vector<double> ang = viewAngles(), outAng(m_g.n_view);
+  ctgpu_geometry go;
+  int rc = CTGPU_ERR_CUDA;
+  if (cudaMalloc(&dIn, inBytes) == cudaSuccess && cudaMalloc(&dOut, outBytes) == cudaSuccess &&
+      cudaMemcpy(dIn, m_data.data(), inBytes, cudaMemcpyHostToDevice) == cudaSuccess)
+    rc = ctgpu_interpolate_to_parallel(&m_g, dIn, m_pitch, ang.data(), dOut, q->m_pitch, &go,
+                                       outAng.data(), nullptr);
+  if (rc == CTGPU_OK) rc = ctgpu_sync(nullptr);
+  if (rc == CTGPU_OK && cudaMemcpy(q->m_data.data(), dOut, outBytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = CTGPU_ERR_CUDA;
+  cudaFree(dIn);
+  cudaFree(dOut);
+  if (rc != CTGPU_OK) {
+    std::fprintf(stderr, "interpolateToParallel: %s\n", ctgpu_last_error());
+    delete q;
+    return nullptr;
+  }
+  q->m_g = go;
+  for (int v = 0; v < m_g.n_view; v++) q->m_views[v].setViewAngle(outAng[v]);
+  q->m_calcTime = 0;
+  q->m_remark = m_remark + "; Interpolate to Parallel";
+  return q;
+}
+
 // ============================================================== ImageFile ==
 ImageFile::ImageFile()
     : m_nx(0), m_ny(0), m_incKnown(false), m_extKnown(false), m_incX(0), m_incY(0), m_minX(0),
@@ -529,11 +559,14 @@ Reconstructor::Reconstructor(const Projections& proj, ImageFile& im, const char*
                              double param, const char* method, int zeropad, const char* gen,
                              const char* interp, int interpF, const char* bp, int,
                              ReconstructionROI* roi, bool rebin, SGP*)
-    : m_proj(proj), m_im(im), m_h(nullptr), m_dSino(nullptr), m_dImage(nullptr), m_fail(false),
-      m_uploaded(false), m_started(false) {
-  if (rebin) {
+    : m_rebinned(rebin && proj.geometry() != CTGPU_GEOMETRY_PARALLEL ? proj.interpolateToParallel()
+                                                                     : nullptr),
+      m_proj(m_rebinned ? *m_rebinned : proj), m_im(im), m_h(nullptr), m_dSino(nullptr),
+      m_dImage(nullptr), m_fail(false), m_uploaded(false), m_started(false) {
+  // reconstruct.cpp:56: rebinToParallel reconstructs interpolateToParallel()
+  if (rebin && proj.geometry() != CTGPU_GEOMETRY_PARALLEL && !m_rebinned) {
     m_fail = true;
-    m_failMessage = "rebinning to parallel geometry is not part of this library";
+    m_failMessage = std::string("interpolateToParallel: ") + last_err();
     return;
   }
   ctgpu_roi r;
@@ -556,6 +589,7 @@ Reconstructor::Reconstructor(const Projections& proj, ImageFile& im, const char*
   }
 }
 Reconstructor::~Reconstructor() {
+  delete m_rebinned;
   ctgpu_recon_destroy(m_h);
   cudaFree(m_dSino);
   cudaFree(m_dImage);

@@ -252,6 +252,22 @@ def halfscan_feather(geometry, sino, stream=None, equilinear=False):
     return sino
 
 
+def interpolate_to_parallel(geometry, sino, angles, stream=None):
+    """Projections::interpolateToParallel of a device fan-beam sinogram:
+    returns (parallel sinogram, its Geometry, its view angles)."""
+    torch = _torch()
+    ang = np.ascontiguousarray(angles, np.float64)
+    out = torch.zeros((geometry.n_view, pitch_for(geometry.n_det)), dtype=torch.float32,
+                      device=sino.device)
+    g2 = Geometry()
+    oa = np.zeros(geometry.n_view, np.float64)
+    check(lib().ctgpu_interpolate_to_parallel(C.byref(geometry), _ptr(sino), sino.shape[1],
+                                              ang.ctypes.data_as(C.c_void_p), _ptr(out),
+                                              out.shape[1], C.byref(g2),
+                                              oa.ctypes.data_as(C.c_void_p), stream_handle(stream)))
+    return out, g2, oa
+
+
 class HelicalPlan:
     """Helical180LI (+ HalfScanFeather) at many interpolation views of one data
     set (ctgpu_helical_plan): tables once, all slices in one launch."""

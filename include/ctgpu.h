@@ -265,6 +265,16 @@ int ctgpu_batch_run(ctgpu_batch* b, void* stream);
 int ctgpu_batch_shape(const ctgpu_batch* b, int* blocks_per_sm, int* views_per_stage);
 void ctgpu_batch_destroy(ctgpu_batch* b);
 
+/* Projections::interpolateToParallel (libctsim/projections.cpp:1250-1328),
+ * what Reconstructor's bRebinToParallel does (reconstruct.cpp:56): fan-beam
+ * d_sino [n_view][pitch] with its view angles -> parallel projections
+ * d_out [n_view][out_pitch] over 2 pi (rot_inc 2 pi / n_view), detectors
+ * spanning the view diameter; g_out receives their geometry and
+ * h_out_angles[n_view] their view angles.  Parallel input is copied. */
+int ctgpu_interpolate_to_parallel(const ctgpu_geometry* g, const float* d_sino, int sino_pitch,
+                                  const double* h_view_angles, float* d_out, int out_pitch,
+                                  ctgpu_geometry* g_out, double* h_out_angles, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Helical -- replaces Projections::Helical180LI / Helical180LI_Equiangular */
 /* and HalfScanFeather (libctsim/projections.cpp:200-439)                     */

@@ -137,6 +137,9 @@ class Projections {
   bool write(const std::string& filename) { return write(filename.c_str()); }
   int Helical180LI(int interpolation_view);   // 0 ok, 1 not enough data, 2 bad geometry
   int HalfScanFeather();
+  // projections.cpp:1250-1328: a new parallel-beam Projections (the caller
+  // deletes it), or this object itself for parallel data; null on failure
+  Projections* interpolateToParallel() const;
   DetectorArray& getDetectorArray(int iview) { return m_views[iview]; }
   const DetectorArray& getDetectorArray(int iview) const { return m_views[iview]; }
   int nView() const { return m_g.n_view; }
@@ -271,6 +274,7 @@ class Reconstructor {
   void postProcessing();
 
  private:
+  Projections* m_rebinned;    // owned: interpolateToParallel() of the input, or null
   const Projections& m_proj;
   ImageFile& m_im;
   ctgpu_recon* m_h;

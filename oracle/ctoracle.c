@@ -1484,6 +1484,101 @@ int ora_halfscan_feather(const ora_geom* g, float* data, int nView) {
 }
 
 /* ------------------------------------------------------------------------- */
+/* Projections::interpolateToParallel (projections.cpp:1250-1328) with      */
+/* ParallelRaysums (:1339-1469) and LinearInterpolator (interpolator.h:187) */
+/* ------------------------------------------------------------------------- */
+typedef struct { double theta, t, raysum; } rb_coord;
+
+static int rb_compare_t(const void* pa, const void* pb) {   /* compareByT */
+  const rb_coord* a = pa;
+  const rb_coord* b = pb;
+  if (a->t == b->t) return a->theta < b->theta ? -1 : (a->theta > b->theta ? 1 : 0);
+  return a->t < b->t ? -1 : 1;
+}
+
+static double normalize_angle(double th) {   /* mathfuncs.cpp:72-81 */
+  while (th < 0.) th += O_TWOPI;
+  while (th >= O_TWOPI) th -= O_TWOPI;
+  return th;
+}
+
+/* LinearInterpolator::interpolate with x given, zero-outside off */
+static double lin_interp(const double* x, const double* y, int n, double dX, int* lastFloor) {
+  int iLower = -1, iUpper = n;
+  if (lastFloor && *lastFloor >= 0 && x[*lastFloor] < dX) iLower = *lastFloor;
+  while (iUpper - iLower > 1) {
+    int iMiddle = (iUpper + iLower) >> 1;
+    if (dX >= x[iMiddle]) iLower = iMiddle;
+    else iUpper = iMiddle;
+  }
+  if (dX == x[0]) return y[0];
+  if (dX < x[0]) return y[0];
+  if (dX == x[n - 1]) return y[n - 1];
+  if (dX > x[n - 1]) return y[n - 1];
+  if (iLower < 0 || iLower >= n) return 0;
+  if (lastFloor) *lastFloor = iLower;
+  return y[iLower] + (y[iUpper] - y[iLower]) * ((dX - x[iLower]) / (x[iUpper] - x[iLower]));
+}
+
+int ora_interpolate_to_parallel(const ora_geom* g, double rotStart, double detStart,
+                                const float* in, const double* viewAngles, float* out,
+                                double* outAngles, double* outHdr) {
+  int nDet = g->nDet, nView = g->nView;
+  if (g->geometry == ORA_GEOM_PARALLEL) return 1;
+  double rotInc = O_TWOPI / nView;
+  double dStart = -g->viewDiameter / 2, dInc = g->viewDiameter / nDet;
+  if (nDet % 2 == 0) dInc = g->viewDiameter / (nDet - 1);
+  rb_coord* c = malloc((size_t)nView * nDet * sizeof(rb_coord));
+  for (int v = 0; v < nView; v++) {
+    double detPos = detStart;
+    for (int d = 0; d < nDet; d++) {
+      rb_coord* pc = &c[(size_t)v * nDet + d];
+      if (g->geometry == ORA_GEOM_EQUILINEAR) {
+        double fan = atan(detPos / g->sourceDetectorLength);
+        pc->theta = viewAngles[v] + fan;
+        pc->t = g->focalLength * sin(fan);
+      } else {
+        pc->theta = viewAngles[v] + detPos;
+        pc->t = g->focalLength * sin(detPos);
+      }
+      pc->theta = normalize_angle(pc->theta);
+      pc->raysum = in[(size_t)v * nDet + d];
+      detPos += g->detInc;
+    }
+  }
+  qsort(c, (size_t)nView * nDet, sizeof(rb_coord), rb_compare_t);
+  double* th = malloc(nView * sizeof(double));
+  double* rs = malloc(nView * sizeof(double));
+  for (int iD = 0; iD < nDet; iD++) {
+    for (int i = 0; i < nView; i++) {
+      th[i] = c[(size_t)iD * nView + i].theta;
+      rs[i] = c[(size_t)iD * nView + i].raysum;
+    }
+    double a = rotStart;
+    int last = -1;
+    for (int iV = 0; iV < nView; iV++, a += rotInc)
+      out[(size_t)iV * nDet + iD] = (float)lin_interp(th, rs, nView, a, &last);
+  }
+  double* dp = malloc(nDet * sizeof(double));
+  double* row = malloc(nDet * sizeof(double));
+  for (int i = 0; i < nDet; i++) dp[i] = c[(size_t)i * nView].t;
+  double a = rotStart;
+  for (int iV = 0; iV < nView; iV++, a += rotInc) {
+    outAngles[iV] = a;
+    for (int i = 0; i < nDet; i++) row[i] = out[(size_t)iV * nDet + i];
+    double pos = dStart;
+    int last = -1;
+    for (int iD = 0; iD < nDet; iD++, pos += dInc)
+      out[(size_t)iV * nDet + iD] = (float)lin_interp(dp, row, nDet, pos, &last);
+  }
+  outHdr[0] = rotInc;
+  outHdr[1] = dStart;
+  outHdr[2] = dInc;
+  free(c); free(th); free(rs); free(dp); free(row);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
 /* Rasteriser: Phantom::convertToImagefile (phantom.cpp:462-542) with        */
 /* PhantomElement::isPointInside (phantom.cpp:913-976)                      */
 /* ------------------------------------------------------------------------- */

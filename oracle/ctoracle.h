@@ -129,6 +129,14 @@ int  ora_helical180li_ex(const ora_geom* g, const float* in, int nViewIn, int in
                          float* out, double* outAngles, int* nViewOut, int allowEquilinear);
 int  ora_halfscan_feather_ex(const ora_geom* g, float* data, int nView, int trueGamma);
 
+/* ---- rebinning to parallel rays: Projections::interpolateToParallel ---- */
+/* fan-beam in [nView][nDet] with its view angles, rotStart and detStart (the
+ * .pj header's) -> out [nView][nDet], outAngles[nView], outHdr = {rotInc,
+ * detStart, detInc} of the parallel projections; 1 for parallel input */
+int ora_interpolate_to_parallel(const ora_geom* g, double rotStart, double detStart,
+                                const float* in, const double* viewAngles, float* out,
+                                double* outAngles, double* outHdr);
+
 /* ---- rasteriser (phm2if) and pixel-image projector ---- */
 void ora_phantom_to_image(const ora_phantom* p, int nx, int ny, double viewRatio, int nsample,
                           double* image, double extent[4], int nThreads);

@@ -91,6 +91,7 @@ def lib():
         _LIB.ora_halfscan_feather_ex.argtypes = [C.POINTER(Geom), p, i, i]
         _LIB.ora_collect_ellipsoids.argtypes = [C.POINTER(_Scanner), p, i, d, d, p, p, i]
         _LIB.ora_ellipse_gradient.argtypes = [C.POINTER(_Scanner), C.POINTER(_Phantom), p, p]
+        _LIB.ora_interpolate_to_parallel.argtypes = [C.POINTER(Geom), d, d, p, p, p, p, p]
         _LIB.ora_phantom_to_image.argtypes = [C.POINTER(_Phantom), i, i, d, i, p, p, i]
         _LIB.ora_project_image.argtypes = [C.POINTER(Geom), p, i, i, p, i, p, i]
         _LIB.ora_frequency_response.argtypes = [i, d, d, d]
@@ -191,6 +192,21 @@ class Scanner:
                                       self.offset_view, start, _ptr(sino), _ptr(ang),
                                       nthreads or nthreads_default())
         return sino, ang
+
+
+def interpolate_to_parallel(geom, rot_start, det_start, sino, angles):
+    """Projections::interpolateToParallel: returns (data [nView, nDet] float32,
+    angles, (rotInc, detStart, detInc))."""
+    sino = np.ascontiguousarray(sino, np.float32)
+    angles = np.ascontiguousarray(angles, np.float64)
+    out = np.zeros_like(sino)
+    oa = np.zeros(sino.shape[0], np.float64)
+    hdr = np.zeros(3, np.float64)
+    rc = lib().ora_interpolate_to_parallel(C.byref(geom), rot_start, det_start, _ptr(sino),
+                                           _ptr(angles), _ptr(out), _ptr(oa), _ptr(hdr))
+    if rc != 0:
+        raise ValueError("interpolateToParallel: parallel input")
+    return out, oa, tuple(hdr)
 
 
 def ellipse_gradient(scanner, gsino):

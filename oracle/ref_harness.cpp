@@ -13,6 +13,8 @@
 //       times Reconstructor over the first NVIEWS views, split across NTHREADS
 //       threads the way the GUI's worker threads do (one Reconstructor and one
 //       private image per thread, images summed: src/threadrecon.cpp:176-255)
+//   ref_harness rebin   IN.pj OUT.pj
+//       Projections::interpolateToParallel (libctsim/projections.cpp:1250-1328)
 //   ref_harness timeraysum PHM NDET NVIEW NRAY GEOM NTHREADS [NVIEWS]
 //       times Scanner::collectProjections over view sub-ranges per thread
 //       (libctsim/scanner.cpp:295-298)
@@ -143,13 +145,24 @@ static int cmdTimeRaysum(int argc, char** argv) {
   return 0;
 }
 
+static int cmdRebin(int argc, char** argv) {
+  if (argc != 4) { fprintf(stderr, "rebin: bad args\n"); return 2; }
+  Projections p;
+  if (!p.read(argv[2])) { fprintf(stderr, "read fail\n"); return 2; }
+  Projections* q = p.interpolateToParallel();
+  bool ok = q->write(argv[3]);
+  if (q != &p) delete q;
+  return ok ? 0 : 2;
+}
+
 int main(int argc, char** argv) {
-  if (argc < 2) { fprintf(stderr, "usage: ref_harness filter|bp|timerec|timeraysum ...\n"); return 2; }
+  if (argc < 2) { fprintf(stderr, "usage: ref_harness filter|bp|timerec|timeraysum|rebin ...\n"); return 2; }
   std::string c = argv[1];
   if (c == "filter") return cmdFilter(argc, argv);
   if (c == "bp") return cmdBackproject(argc, argv);
   if (c == "timerec") return cmdTimeRec(argc, argv);
   if (c == "timeraysum") return cmdTimeRaysum(argc, argv);
+  if (c == "rebin") return cmdRebin(argc, argv);
   fprintf(stderr, "unknown command %s\n", argv[1]);
   return 2;
 }

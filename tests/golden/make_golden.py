@@ -136,6 +136,23 @@ def make_helical(tmp):
     np.savez_compressed(os.path.join(HERE, "helical.npz"), **out)
 
 
+# fan-beam scans rebinned to parallel rays (Projections::interpolateToParallel)
+REBINS = ["shepp_eqa", "shepp_eqa_even", "herman_eql", "herman_eqa", "shepp_eql_ratio"]
+
+
+def make_rebin(tmp):
+    out = {}
+    for name in REBINS:
+        pjf = os.path.join(tmp, name + ".pj")
+        if not os.path.exists(pjf):
+            sc = [s for s in SCANS if s[0] == name][0]
+            run(REF, "phm2pj", pjf, sc[3], sc[4], "--phantom", sc[1], "--geometry", sc[2],
+                "--nray", sc[5], *sc[6])
+        run(HARN, "rebin", pjf, os.path.join(tmp, "rb.pj"))
+        out.update(pj_arrays(name + "/", read_pj(os.path.join(tmp, "rb.pj"))))
+    np.savez_compressed(os.path.join(HERE, "rebin.npz"), **out)
+
+
 def make_raster(tmp):
     out = {}
     for k, (phm, n, ns) in enumerate([("herman", 48, 2), ("shepp-logan", 40, 3)]):
@@ -150,12 +167,16 @@ def main():
     for b in (REF, REF64, HARN):
         if not os.path.exists(b):
             sys.exit("reference not built: run `make -C oracle ref`")
+    only = sys.argv[1:]
     with tempfile.TemporaryDirectory() as tmp:
-        scans = make_scans(tmp)
-        make_recons(tmp, scans)
-        make_filters(tmp)
-        make_helical(tmp)
-        make_raster(tmp)
+        if not only:
+            scans = make_scans(tmp)
+            make_recons(tmp, scans)
+            make_filters(tmp)
+            make_helical(tmp)
+            make_raster(tmp)
+        if not only or "rebin" in only:
+            make_rebin(tmp)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print("%-14s %8d bytes" % (f, os.path.getsize(os.path.join(HERE, f))))

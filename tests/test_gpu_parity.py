@@ -311,3 +311,25 @@ def test_raysums_batch_equals_single(gpu, geo, nray):
         cg.sync()
         assert np.array_equal(ang, ang_b)
         assert torch.equal(one[:, :157], batch[i, :, :157]), i
+
+
+@pytest.mark.parametrize("name", ["shepp_eqa", "shepp_eqa_even", "herman_eql", "herman_eqa",
+                                  "shepp_eql_ratio"])
+def test_interpolate_to_parallel_matches_reference(gpu, golden, name):
+    """Projections::interpolateToParallel on the device against the reference's
+    own output (ref_harness rebin on the reference's scan)."""
+    torch, cg, device = gpu
+    d, r = golden("scans"), golden("rebin")
+    g = geom_from_hdr(cg, d[name + "/hdr"])
+    data = d[name + "/data"]
+    sino = torch.zeros((g.n_view, device.pitch_for(g.n_det)), device="cuda")
+    sino[:, :g.n_det] = torch.from_numpy(data).cuda()
+    out, g2, ang = device.interpolate_to_parallel(g, sino, d[name + "/angles"])
+    cg.sync()
+    ref, rh = r[name + "/data"], r[name + "/hdr"]
+    np.testing.assert_array_equal(ang, r[name + "/angles"])
+    assert (g2.geometry, g2.rot_inc, g2.det_start, g2.det_inc) == (0, rh[4], rh[5], rh[6])
+    o = out[:, :g.n_det].cpu().numpy()
+    err = np.abs(o - ref).max() / np.abs(ref).max()
+    print("interpolateToParallel %s: max |err| / max %.3g" % (name, err))
+    assert err <= 1e-6, err

@@ -115,3 +115,19 @@ def test_oracle_projector_is_adjoint_of_backprojector(oracle, golden):
     ax = oracle.project_image(g, x, ang)
     bty = oracle.backproject(g, y, ang, 24, 20, "table", "linear", post_process=False)
     assert abs(np.vdot(ax, y) - np.vdot(x, bty)) < 1e-12 * abs(np.vdot(ax, y))
+
+
+@pytest.mark.parametrize("name", ["shepp_eqa", "shepp_eqa_even", "herman_eql", "herman_eqa",
+                                  "shepp_eql_ratio"])
+def test_oracle_interpolate_to_parallel(oracle, golden, name):
+    """ora_interpolate_to_parallel bit for bit against the reference's
+    Projections::interpolateToParallel on the same scan."""
+    d, r = golden("scans"), golden("rebin")
+    h = d[name + "/hdr"]
+    g = oracle.Geom(int(h[0]), int(h[1]), int(h[2]), h[4], h[6], h[8], h[9], h[7], h[10])
+    out, ang, hdr = oracle.interpolate_to_parallel(g, h[3], h[5], d[name + "/data"],
+                                                   d[name + "/angles"])
+    rh = r[name + "/hdr"]
+    assert hdr == (rh[4], rh[5], rh[6])
+    np.testing.assert_array_equal(ang, r[name + "/angles"])
+    np.testing.assert_array_equal(out, r[name + "/data"])
