@@ -80,6 +80,20 @@ class Phantom:
             lib().ctgpu_phantom_destroy(self._h)
             self._h = None
 
+    def rasterize(self, nx, ny, view_ratio=1.0, nsample=1):
+        """Phantom::convertToImagefile (phm2if) on the device: returns (image
+        [nx, ny] float32 CUDA tensor, extent (xmin, xmax, ymin, ymax),
+        increment (xinc, yinc))."""
+        import torch
+        img = torch.zeros((nx, ny), dtype=torch.float32, device="cuda")
+        ext = (C.c_double * 4)()
+        inc = (C.c_double * 2)()
+        check(lib().ctgpu_phantom_rasterize(self._h, nx, ny, float(view_ratio), int(nsample),
+                                            C.c_void_p(img.data_ptr()), ext, inc, None))
+        sync()
+        return img, tuple(ext), tuple(inc)
+
+
 
 class Scanner:
     """Scanner(phm, geometry, nDet, nView, offsetView, nSample, rotAngle, focalLengthRatio,

@@ -66,6 +66,7 @@ SIGNATURES = {
     "ctgpu_phantom_read_file": ([_p, _s], _i),
     "ctgpu_phantom_bounds": ([_p, C.POINTER(_d), C.POINTER(_i)], _i),
     "ctgpu_phantom_destroy": ([_p], None),
+    "ctgpu_phantom_rasterize": ([_p, _i, _i, _d, _i, _p, C.POINTER(_d), C.POINTER(_d), _p], _i),
     "ctgpu_scanner_create": ([_p, _s, _i, _i, _i, _i, _d, _d, _d, _d, _d, _pp], _i),
     "ctgpu_scanner_geometry": ([_p, C.POINTER(Geometry)], _i),
     "ctgpu_collect_projections": ([_p, _p, _i, _i, _i, _i, _p, _i, _p, _p], _i),

@@ -56,6 +56,7 @@ cudaError_t ensure_device(T*& p, size_t& cap, size_t count) {
 struct M3 { double m[3][3]; };
 M3 ident() { M3 r{}; r.m[0][0] = r.m[1][1] = r.m[2][2] = 1; return r; }
 M3 xlat(double x, double y) { M3 r = ident(); r.m[2][0] = x; r.m[2][1] = y; return r; }
+M3 scalem(double sx, double sy) { M3 r = ident(); r.m[0][0] = sx; r.m[1][1] = sy; return r; }
 M3 rotm(double t) {
   M3 r = ident();
   double c = std::cos(t), s = std::sin(t);
@@ -806,6 +807,67 @@ int ctgpu_raysum_ellipse_gradient(ctgpu_scanner* s, const ctgpu_phantom* p,
     for (int j = 0; j < 6; j++) o[j] = g[6 * (size_t)k + j];
     o[4] *= kPi / 180.0;
   }
+  return ok();
+}
+
+int ctgpu_phantom_rasterize(const ctgpu_phantom* p, int nx, int ny, double viewRatio, int nsample,
+                            float* d_image, double extent[4], double increment[2], void* stream) {
+  if (!p || !d_image) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (nx < 2 || ny < 2) return ok();   // phantom.cpp:466-467: nothing is written
+  if (nsample < 1) nsample = 1;
+  // phantom.cpp:473-494 (getDiameterBoundaryCircle: phantom.h:190-194)
+  const double dx = p->xmax - p->xmin, dy = p->ymax - p->ymin;
+  const double xcent = p->xmin + dx / 2, ycent = p->ymin + dy / 2;
+  const double diam = kSqrt2 * (dx > dy ? dx : dy);
+  const double half = viewRatio * (diam / kSqrt2 / 2);
+  const double xmin = xcent - half, xmax = xcent + half, ymin = ycent - half, ymax = ycent + half;
+  const double xinc = (xmax - xmin) / nx, yinc = (ymax - ymin) / ny;
+  if (extent) { extent[0] = xmin; extent[1] = xmax; extent[2] = ymin; extent[3] = ymax; }
+  if (increment) { increment[0] = xinc; increment[1] = yinc; }
+  // PhantomElement ctor's phantom-to-object map (phantom.cpp:629-655)
+  std::vector<RasterElem> el(p->elems.size());
+  for (size_t k = 0; k < el.size(); k++) {
+    const PElem& e = p->elems[k];
+    M3 m = mul(mul(xlat(-e.cx, -e.cy), rotm(-e.rot)), scalem(1 / e.u, 1 / e.v));
+    RasterElem r{};
+    std::memcpy(r.m, m.m, sizeof(r.m));
+    r.u = e.u;
+    r.v = e.v;
+    r.atten = e.atten;
+    r.type = e.type;
+    el[k] = r;
+  }
+  std::vector<double> xc(nx), yr(ny);
+  double x = xmin;
+  for (int ix = 0; ix < nx; ix++, x += xinc) xc[ix] = x;
+  double y = ymin;
+  for (int iy = 0; iy < ny; iy++, y += yinc) yr[iy] = y;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t be = sizeof(RasterElem) * (el.size() ? el.size() : 1);
+  unsigned char* blk = nullptr;
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&blk), be + sizeof(double) * (nx + ny), st));
+  cudaError_t err = cudaSuccess;
+  if (!el.empty()) err = cudaMemcpyAsync(blk, el.data(), sizeof(RasterElem) * el.size(), cudaMemcpyHostToDevice, st);
+  if (err == cudaSuccess) err = cudaMemcpyAsync(blk + be, xc.data(), sizeof(double) * nx, cudaMemcpyHostToDevice, st);
+  if (err == cudaSuccess)
+    err = cudaMemcpyAsync(blk + be + sizeof(double) * nx, yr.data(), sizeof(double) * ny, cudaMemcpyHostToDevice, st);
+  RasterLaunch L{};
+  L.nx = nx;
+  L.ny = ny;
+  L.nsample = nsample;
+  L.nElem = (int)el.size();
+  L.elems = reinterpret_cast<const RasterElem*>(blk);
+  L.xcol = reinterpret_cast<const double*>(blk + be);
+  L.yrow = reinterpret_cast<const double*>(blk + be) + nx;
+  L.kxinc = xinc / nsample;
+  L.kyinc = yinc / nsample;
+  L.kxofs = L.kxinc / 2;
+  L.kyofs = L.kyinc / 2;
+  L.factor = 1.0 / static_cast<double>(nsample * nsample);
+  L.image = d_image;
+  if (err == cudaSuccess) err = launch_raster(L, st);
+  cudaFreeAsync(blk, st);
+  CUDA_TRY(err);
   return ok();
 }
 

@@ -138,6 +138,22 @@ struct HelicalSlicesLaunch {
   size_t outSliceStride;
   unsigned int* status;
 };
+// Phantom::convertToImagefile on the device (k_raysum.cu)
+struct RasterElem {
+  double m[3][3];     // PhantomElement's phantom-to-object map (row vectors)
+  double u, v, atten;
+  int type, pad;
+};
+struct RasterLaunch {
+  int nx, ny, nsample, nElem;
+  const RasterElem* elems;   // list order
+  const double* xcol;        // nx: each column's x, accumulated as the reference does
+  const double* yrow;        // ny
+  double kxinc, kyinc, kxofs, kyofs, factor;
+  float* image;              // [nx][ny]
+};
+cudaError_t launch_raster(const RasterLaunch& L, cudaStream_t s);
+
 // Projections::interpolateToParallel on the device (k_rebin.cu)
 struct RebinLaunch {
   int nDet, nView, pitch, outPitch, sortN, pad;

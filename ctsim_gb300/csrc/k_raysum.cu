@@ -631,3 +631,70 @@ cudaError_t launch_raysum_ellipse_grad(const RaysumLaunch& L, const float* gsino
 }
 
 }  // namespace ctgpu
+
+// ---------------------------------------------------------------------------
+// Phantom::convertToImagefile (libctsim/phantom.cpp:462-542), what phm2if does:
+// each pixel is the mean over nsample x nsample points of the summed
+// attenuation of the elements containing the point
+// (PhantomElement::isPointInside, phantom.cpp:913-976).  One thread per pixel;
+// the point coordinates are accumulated by the reference's own sequential
+// additions (column and row starts from the host), every test is its FP64
+// affine map, and the FP32 pixel is updated once per element in list order
+// with the reference's FP32-image roundings.
+// ---------------------------------------------------------------------------
+namespace ctgpu {
+
+__device__ __forceinline__ bool raster_inside(const RasterElem& e, double x, double y) {
+  const double xo = x * e.m[0][0] + y * e.m[1][0] + e.m[2][0];
+  const double yo = x * e.m[0][1] + y * e.m[1][1] + e.m[2][1];
+  double xs = xo, ys = yo;
+  switch (e.type) {
+    case kRect: return !(xo > 1. || xo < -1. || yo > 1. || yo < -1.);
+    case kTriangle: return !(yo < 0. || yo > 1. - xo || yo > 1. + xo);
+    case kEllipse:
+      if (xo > 1. || xo < -1. || yo > 1. || yo < -1.) return false;
+      return !(xo * xo + yo * yo > 1.);
+    case kSegment:
+      if (xo > 1. || xo < -1. || yo > 0.) return false;
+      xs *= e.u;
+      ys *= e.v;
+      return !(xs * xs + (ys - e.v) * (ys - e.v) > e.u * e.u + e.v * e.v);
+    case kSector:
+      if (xo > 1. || xo < -1. || yo > 1.) return false;
+      if (yo > 1. - xo || yo > 1. + xo) return false;
+      xs *= e.u;
+      ys *= e.v;
+      return !(xs * xs + (ys - e.v) * (ys - e.v) > e.u * e.u + e.v * e.v);
+    default: return false;
+  }
+}
+
+__global__ void raster_kernel(RasterLaunch L) {
+  const int ix = blockIdx.x;
+  const double x = L.xcol[ix];
+  for (int iy = threadIdx.x; iy < L.ny; iy += blockDim.x) {
+    const double y = L.yrow[iy];
+    float pix = 0.f;
+    for (int k = 0; k < L.nElem; k++) {
+      const RasterElem& e = L.elems[k];
+      double a = 0;
+      double xi = x + L.kxofs;
+      for (int kx = 0; kx < L.nsample; kx++, xi += L.kxinc) {
+        double yi = y + L.kyofs;
+        for (int ky = 0; ky < L.nsample; ky++, yi += L.kyinc)
+          if (raster_inside(e, xi, yi)) a += e.atten;
+      }
+      pix = (float)((double)pix + a);
+    }
+    if (L.nsample > 1) pix = (float)((double)pix * L.factor);
+    L.image[(size_t)ix * L.ny + iy] = pix;
+  }
+}
+
+cudaError_t launch_raster(const RasterLaunch& L, cudaStream_t s) {
+  if (L.nx <= 0 || L.ny <= 0) return cudaSuccess;
+  raster_kernel<<<L.nx, 128, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+}  // namespace ctgpu

@@ -77,6 +77,14 @@ int ctgpu_phantom_add_element(ctgpu_phantom* p, const char* type, double cx, dou
 int ctgpu_phantom_read_file(ctgpu_phantom* p, const char* filename);
 /* xmin, xmax, ymin, ymax of the union of element bounding boxes (phantom.cpp:250-253) */
 int ctgpu_phantom_bounds(const ctgpu_phantom* p, double bounds[4], int* n_elements);
+/* Phantom::convertToImagefile (phantom.cpp:462-542), what phm2if does: each
+ * pixel of d_image [nx][ny] (column-major, FP32 as ImageFile) is the mean
+ * over nsample x nsample points of the summed attenuation of the elements
+ * containing the point; extent (xmin, xmax, ymin, ymax) and increment
+ * receive the image axes.  Images smaller than 2 x 2 are left untouched. */
+int ctgpu_phantom_rasterize(const ctgpu_phantom* p, int nx, int ny, double view_ratio,
+                            int nsample, float* d_image, double extent[4], double increment[2],
+                            void* stream);
 void ctgpu_phantom_destroy(ctgpu_phantom* p);
 
 /* ------------------------------------------------------------------------ */

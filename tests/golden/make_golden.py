@@ -155,10 +155,13 @@ def make_rebin(tmp):
 
 def make_raster(tmp):
     out = {}
-    for k, (phm, n, ns) in enumerate([("herman", 48, 2), ("shepp-logan", 40, 3)]):
+    for k, (phm, n, ns) in enumerate([("herman", 48, 2), ("shepp-logan", 40, 3),
+                                      ("shepp-logan", 64, 1)]):
         f = os.path.join(tmp, "p.if")
         run(REF64, "phm2if", f, n, n, "--phantom", phm, "--nsample", ns)
         out["%d/image" % k] = read_if(f).data
+        run(REF, "phm2if", f, n, n, "--phantom", phm, "--nsample", ns)
+        out["%d/image32" % k] = read_if(f).data
         out["%d/cfg" % k] = np.array([phm, n, ns], dtype=object)
     np.savez_compressed(os.path.join(HERE, "raster.npz"), **out)
 
@@ -177,6 +180,8 @@ def main():
             make_raster(tmp)
         if not only or "rebin" in only:
             make_rebin(tmp)
+        if "raster" in only:
+            make_raster(tmp)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print("%-14s %8d bytes" % (f, os.path.getsize(os.path.join(HERE, f))))

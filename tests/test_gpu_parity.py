@@ -333,3 +333,21 @@ def test_interpolate_to_parallel_matches_reference(gpu, golden, name):
     err = np.abs(o - ref).max() / np.abs(ref).max()
     print("interpolateToParallel %s: max |err| / max %.3g" % (name, err))
     assert err <= 1e-6, err
+
+
+def test_rasterize_matches_reference(gpu, golden):
+    """Phantom::convertToImagefile (phm2if) on the device: bit for bit against
+    the reference's FP32-image build, and within FP32 rounding of its FP64
+    build."""
+    torch, cg, device = gpu
+    r = golden("raster")
+    k = 0
+    while "%d/cfg" % k in r:
+        phm, n, ns = r["%d/cfg" % k]
+        img, ext, inc = cg.Phantom(str(phm)).rasterize(int(n), int(n), 1.0, int(ns))
+        a = img.cpu().numpy()
+        np.testing.assert_array_equal(a, r["%d/image32" % k])
+        ref64 = r["%d/image" % k]
+        assert np.abs(a - ref64).max() <= 1e-6 * max(np.abs(ref64).max(), 1e-30)
+        k += 1
+    assert k == 3

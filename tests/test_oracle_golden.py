@@ -99,7 +99,7 @@ def test_oracle_helical_matches_reference(oracle, golden):
 
 def test_oracle_raster_matches_reference(oracle, golden):
     d = golden("raster")
-    for k in range(2):
+    for k in range(3):
         phm, n, ns = d["%d/cfg" % k]
         img, _ = oracle.phantom_to_image(oracle.Phantom(phm), int(n), int(n), 1.0, int(ns))
         np.testing.assert_allclose(img, d["%d/image" % k], rtol=0, atol=1e-12)
