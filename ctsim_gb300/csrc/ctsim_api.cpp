@@ -339,6 +339,29 @@ int Projections::HalfScanFeather() {   // projections.cpp:369-439
   return 0;
 }
 
+bool Phantom::isUnitPulse() const { return !strcasecmp(m_name.c_str(), "unit-pulse"); }
+
+void Phantom::convertToImagefile(ImageFile& im, double viewRatio, int nsample, int) const {
+  const int nx = im.nx(), ny = im.ny();
+  if (nx < 2 || ny < 2) return;   // phantom.cpp:466-467
+  float* d = nullptr;
+  double ext[4], inc[2];
+  size_t bytes = sizeof(float) * (size_t)nx * ny;
+  int rc = CTGPU_ERR_CUDA;
+  if (cudaMalloc(&d, bytes) == cudaSuccess)
+    rc = ctgpu_phantom_rasterize(m_h, nx, ny, viewRatio, nsample, d, ext, inc, nullptr);
+  if (rc == CTGPU_OK) rc = ctgpu_sync(nullptr);
+  if (rc == CTGPU_OK && cudaMemcpy(im.data(), d, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = CTGPU_ERR_CUDA;
+  cudaFree(d);
+  if (rc != CTGPU_OK) {
+    std::fprintf(stderr, "convertToImagefile: %s\n", ctgpu_last_error());
+    return;
+  }
+  im.setAxisExtent(ext[0], ext[1], ext[2], ext[3]);
+  im.setAxisIncrement(inc[0], inc[1]);
+}
+
 Projections* Projections::interpolateToParallel() const {   // projections.cpp:1250-1328
   if (m_g.geometry == CTGPU_GEOMETRY_PARALLEL) return const_cast<Projections*>(this);
   Projections* q = new Projections(m_g.n_view, m_g.n_det);

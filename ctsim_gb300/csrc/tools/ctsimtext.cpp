@@ -322,6 +322,118 @@ int pjHinterp_main(int argc, char* const argv[]) {
   return 0;
 }
 
+// ------------------------------------------------------------------ phm2if --
+// tools/phm2if.cpp: rasterise a phantom (phantom modes; the filter-response
+// mode, ImageFile::filterResponse, is not part of this library)
+void phm2if_usage(const char* program) {
+  std::cout << "phm2if_usage: " << base_name(program) << " outfile nx ny [--phantom phantom-name] [--phmfile filename] [--filter filter-name] [OPTIONS]\n";
+  std::cout << "Generates phantom image by rasterizing the phantom\n\n";
+  std::cout << "     outfile         Name of output file for image\n";
+  std::cout << "     nx              Number of pixels X-axis\n";
+  std::cout << "     ny              Number of pixels Y-axis\n";
+  std::cout << "     --view-ratio    View diameter to phantom diameter ratio (default = 1)\n";
+  std::cout << "     --phantom       Phantom to use for projection\n";
+  std::cout << "        herman       Herman head phantom\n";
+  std::cout << "        shepp-logan  Shepp-Logan head phantom\n";
+  std::cout << "        unit-pulse    Unit pulse phantom\n";
+  std::cout << "     --phmfile       Generate Phantom from phantom file\n";
+  std::cout << "     --desc          Description of raysum\n";
+  std::cout << "     --nsample       Number of samples per axis per pixel (default = 1)\n";
+  std::cout << "     --verbose       Verbose mode\n";
+  std::cout << "     --help          Print this help message\n";
+}
+
+int phm2if_main(int argc, char* const argv[]) {
+  enum { O_PHANTOM, O_DESC, O_NSAMPLE, O_FILTER, O_VIEW_RATIO, O_TRACE, O_VERBOSE, O_HELP,
+         O_PHMFILE, O_FILTER_DOMAIN, O_FILTER_BW, O_FILTER_PARAM, O_DEBUG, O_VERSION };
+  const struct option phm2if_options[] = {
+      {"phantom", 1, 0, O_PHANTOM},         {"phmfile", 1, 0, O_PHMFILE},
+      {"desc", 1, 0, O_DESC},               {"nsample", 1, 0, O_NSAMPLE},
+      {"filter", 1, 0, O_FILTER},           {"filter-domain", 1, 0, O_FILTER_DOMAIN},
+      {"filter-bw", 1, 0, O_FILTER_BW},     {"filter-param", 1, 0, O_FILTER_PARAM},
+      {"trace", 1, 0, O_TRACE},             {"view-ratio", 1, 0, O_VIEW_RATIO},
+      {"verbose", 0, 0, O_VERBOSE},         {"debug", 0, 0, O_DEBUG},
+      {"help", 0, 0, O_HELP},               {"version", 0, 0, O_VERSION},
+      {0, 0, 0, 0}};
+  std::string phmName, phmFile, filterName, desc;
+  int nsample = 1;
+  double viewRatio = 1.;
+  bool verbose = false;
+  char* endptr = nullptr;
+  optind = 0;
+  while (1) {
+    int c = getopt_long(argc, argv, "", phm2if_options, nullptr);
+    if (c == -1) break;
+    switch (c) {
+      case O_PHANTOM: phmName = optarg; break;
+      case O_PHMFILE: phmFile = optarg; break;
+      case O_VERBOSE: verbose = true; break;
+      case O_DEBUG: case O_TRACE: case O_FILTER_DOMAIN: case O_FILTER_BW: case O_FILTER_PARAM: break;
+      case O_FILTER: filterName = optarg; break;
+      case O_DESC: desc = optarg; break;
+      case O_VIEW_RATIO:
+        viewRatio = strtod(optarg, &endptr);
+        if (endptr != optarg + strlen(optarg)) {
+          std::cerr << "Error setting --view-ratio to " << optarg << "\n";
+          phm2if_usage(argv[0]);
+          return 1;
+        }
+        break;
+      case O_NSAMPLE:
+        nsample = (int)strtol(optarg, &endptr, 10);
+        if (endptr != optarg + strlen(optarg)) {
+          std::cerr << "Error setting --nsample to " << optarg << "\n";
+          phm2if_usage(argv[0]);
+          return 1;
+        }
+        break;
+      case O_VERSION: std::cout << "Version 5.2.0 (GB300)" << std::endl; return 0;
+      case O_HELP: case '?': phm2if_usage(argv[0]); return 0;
+      default: phm2if_usage(argv[0]); return 1;
+    }
+  }
+  if (phmName == "" && filterName == "" && phmFile == "") {
+    std::cerr << "No phantom defined\n" << std::endl;
+    phm2if_usage(argv[0]);
+    return 1;
+  }
+  if (optind + 3 != argc) { phm2if_usage(argv[0]); return 1; }
+  const char* out = argv[optind];
+  int nx = (int)strtol(argv[optind + 1], &endptr, 10);
+  if (endptr != argv[optind + 1] + strlen(argv[optind + 1])) { phm2if_usage(argv[0]); return 1; }
+  int ny = (int)strtol(argv[optind + 2], &endptr, 10);
+  if (endptr != argv[optind + 2] + strlen(argv[optind + 2])) { phm2if_usage(argv[0]); return 1; }
+  if (filterName != "" && phmName == "" && phmFile == "") {
+    std::cerr << "phm2if --filter (filter-response images) is not part of this library\n";
+    return 1;
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  std::ostringstream oss;
+  oss << "phm2if: nx=" << nx << ", ny=" << ny << ", viewRatio=" << viewRatio << ", nsample=" << nsample << ", ";
+  if (phmFile != "") oss << "phantomFile=" << phmFile;
+  else oss << "phantom=" << phmName;
+  if (desc != "") oss << ": " << desc;
+  Phantom phm;
+  if (phmName != "") {
+    phm.createFromPhantom(phmName.c_str());
+    if (phm.fail()) {
+      std::cout << phm.failMessage() << std::endl << std::endl;
+      phm2if_usage(argv[0]);
+      return 1;
+    }
+  }
+  if (phmFile != "") phm.createFromFile(phmFile.c_str());
+  if (verbose) std::cout << "Rasterize Phantom to Image\n" << std::endl;
+  ImageFile im(nx, ny);
+  if (phm.isUnitPulse()) im.getArray()[nx / 2][ny / 2] = 1.f;
+  else phm.convertToImagefile(im, viewRatio, nsample);
+  double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  im.labelAdd(oss.str(), t);
+  im.fileWrite(out);
+  if (verbose) std::cout << "Time to rasterize phantom: " << t << " seconds\n";
+  return 0;
+}
+
 // ------------------------------------------------------------------ pjinfo --
 int pjinfo_main(int argc, char* const argv[]) {
   if (argc < 2) {
@@ -345,8 +457,9 @@ int dispatch(int argc, char* argv[]) {
   if (!strcasecmp(f, "pjrec")) return pjrec_main(argc, argv);
   if (!strcasecmp(f, "pjHinterp")) return pjHinterp_main(argc, argv);
   if (!strcasecmp(f, "pjinfo")) return pjinfo_main(argc, argv);
+  if (!strcasecmp(f, "phm2if")) return phm2if_main(argc, argv);
   std::cout << "Unknown function name: " << f << "\n"
-            << "usage: ctgpu_ctsimtext phm2pj|pjrec|pjHinterp|pjinfo args...\n";
+            << "usage: ctgpu_ctsimtext phm2pj|pjrec|pjHinterp|pjinfo|phm2if args...\n";
   return 1;
 }
 

@@ -32,6 +32,8 @@ typedef float* ImageFileColumn;
 typedef float** ImageFileArray;
 class SGP;                         // graphics device; unused
 
+class ImageFile;
+
 class Phantom {
  public:
   Phantom();
@@ -51,6 +53,9 @@ class Phantom {
   double ymax() const;
   double maxAxisLength() const;
   double getDiameterBoundaryCircle() const;   // include/phantom.h:190-194
+  bool isUnitPulse() const;                    // composition P_UNIT_PULSE
+  // phantom.cpp:455-542: rasterise into im (all columns), on the device
+  void convertToImagefile(ImageFile& im, double dViewRatio, int nsample, int trace = 0) const;
   ctgpu_phantom* handle() const { return m_h; }
 
  private:

@@ -72,3 +72,23 @@ def test_cli_errors_match_reference(tool, tmp_path):
     assert rc == 1 and "Invalid phantom name nope" in out
     rc, out = run(tool, "pjrec", tmp_path / "missing.pj", tmp_path / "x.if", 8, 8)
     assert rc == 1 and "Unable to read projectfile" in out
+
+
+def test_phm2if_matches_reference(tool, golden, tmp_path):
+    """phm2if (Phantom::convertToImagefile) writes the reference's FP32 image
+    bit for bit, with the image axes and history label."""
+    from ctsim_gb300.fileio import read_if
+    r = golden("raster")
+    for k in range(3):
+        phm, n, ns = r["%d/cfg" % k]
+        f = tmp_path / ("p%d.if" % k)
+        rc, out = run(tool, "phm2if", f, int(n), int(n), "--phantom", str(phm), "--nsample",
+                      int(ns))
+        assert rc == 0, out
+        im = read_if(f)
+        assert im.nx == int(n) and im.pixel_size == 4
+        np.testing.assert_array_equal(im.data, r["%d/image32" % k])
+        assert im.labels[-1][1].startswith("phm2if: nx=%d, ny=%d, viewRatio=1, nsample=%d, phantom=%s"
+                                           % (int(n), int(n), int(ns), phm))
+    rc, out = run(tool, "phm2if", tmp_path / "x.if", 8, 8)
+    assert rc == 1 and "No phantom defined" in out
