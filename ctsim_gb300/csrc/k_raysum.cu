@@ -40,6 +40,9 @@ struct ElemView {
   float ra, rb;      // parallel: ray direction in the element frame
   int live;          // 0: no ray of this view can meet the element
   float rin;         // radius of the outline box's inscribed circle, less the margin
+  // E = (ra/u)^2 + (rb/v)^2 of a unit ray direction (rx, ry) as a quadratic
+  // form, E = qa rx^2 + qb rx ry + qc ry^2, and u v (ellipse chords)
+  float qa, qb, qc, uv;
 };
 static_assert(sizeof(ElemView) % 16 == 0, "ElemView records keep 16-byte alignment");
 
@@ -82,18 +85,23 @@ __device__ __forceinline__ float half_chord(float r, float s) {
   return sqrtf((r - as) * (r + as));
 }
 
-// Chord of the line {P + t (ra,rb)} (element frame, unit direction) with the
-// element; P is the foot of the perpendicular from the element centre at
-// signed distance rho.
-__device__ float element_chord(const ElemView& e, float rho, float ra, float rb) {
+// sqrt(x) for x >= 0 from the hardware reciprocal square root (a few ulp)
+__device__ __forceinline__ float sqrt_fast(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
+
+// Chord of the line with unit direction (rx, ry) (world frame; (ra, rb) in the
+// element frame) at signed distance rho from the element centre.  Ellipse:
+// with E = (ra/u)^2 + (rb/v)^2 the half-chord reaches h = u v sqrt(E), and the
+// chord is 2 sqrt(h^2 - rho^2) / (E u v) (factored as (h - |rho|)(h + |rho|)).
+__device__ float element_chord(const ElemView& e, float rho, float rx, float ry, float ra,
+                               float rb) {
   float u = e.u, v = e.v;
   if (e.type == kEllipse) {
-    float xa = ra / u, xb = rb / v;
-    float E = fmaf(xa, xa, xb * xb);
-    float uv = u * v;
-    float h = uv * sqrtf(E);
-    float hc = half_chord(h, rho);
-    return hc == 0.f ? 0.f : __fdividef(2.f * hc, E * uv);
+    const float E = fmaf(rx * rx, e.qa, fmaf(rx * ry, e.qb, ry * ry * e.qc));
+    const float h = e.uv * sqrt_fast(E);
+    const float as = fabsf(rho);
+    if (as >= h) return 0.f;
+    const float hc = sqrt_fast((h - as) * (h + as));
+    return __fdividef(2.f * hc, E * e.uv);
   }
   float px = rho * rb, py = -rho * ra;
   float lo = -INFINITY, hi = INFINITY;
@@ -151,36 +159,15 @@ __device__ bool clip_rect_fp64(double x1, double y1, double x2, double y2, const
 }
 
 // FP32 test of the infinite ray line against the element's outline box:
-// +1 clearly hits, -1 clearly misses, 0 within the rounding margin.
-__device__ __forceinline__ int box_test(const ElemView& e, float rho, float rx, float ry) {
-  float rhob = rho + (rx * e.dcby - ry * e.dcbx);
-  float px = rhob * ry, py = -rhob * rx;   // foot from the box centre (world frame)
-  float margin = 1e-5f * (e.hx + e.hy) + 1e-9f;
-  float lo = -INFINITY, hi = INFINITY;
-  bool amb = false;
-  // x slabs
-  if (fabsf(rx) > 0.f) {
-    float t1 = __fdiv_rn(-e.hx - px, rx), t2 = __fdiv_rn(e.hx - px, rx);
-    lo = fmaxf(lo, fminf(t1, t2));
-    hi = fminf(hi, fmaxf(t1, t2));
-  } else {
-    float b = e.hx - fabsf(px);
-    if (b < -margin) return -1;
-    if (b <= margin) amb = true;
-  }
-  if (fabsf(ry) > 0.f) {
-    float t1 = __fdiv_rn(-e.hy - py, ry), t2 = __fdiv_rn(e.hy - py, ry);
-    lo = fmaxf(lo, fminf(t1, t2));
-    hi = fminf(hi, fmaxf(t1, t2));
-  } else {
-    float b = e.hy - fabsf(py);
-    if (b < -margin) return -1;
-    if (b <= margin) amb = true;
-  }
-  float gap = hi - lo;
-  if (gap < -margin) return -1;
-  if (amb || gap <= margin) return 0;
-  return 1;
+// +1 clearly hits, -1 clearly misses, 0 within the rounding margin.  The line
+// at distance |rhob| from the box centre meets the box exactly when
+// |rhob| <= hx |ry| + hy |rx| (the box's half-width along the line's normal).
+__device__ __forceinline__ int box_test(const ElemView& e, float rhob, float rx, float ry) {
+  const float m = fmaf(e.hx, fabsf(ry), e.hy * fabsf(rx)) - fabsf(rhob);
+  const float margin = 1e-5f * (e.hx + e.hy) + 1e-9f;
+  if (m > margin) return 1;
+  if (m < -margin) return -1;
+  return 0;
 }
 
 __device__ __forceinline__ void split_root(double t, int& ti, float& tf) {
@@ -207,6 +194,14 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
   e.hy = pe.hy;
   e.rbox = pe.rbox;
   e.rin = pe.rin;
+  {
+    const double iu2 = 1.0 / (pe.u * pe.u), iv2 = 1.0 / (pe.v * pe.v);
+    const double c = pe.cosr, sn = pe.sinr;
+    e.qa = (float)(c * c * iu2 + sn * sn * iv2);
+    e.qb = (float)(2.0 * c * sn * (iu2 - iv2));
+    e.qc = (float)(sn * sn * iu2 + c * c * iv2);
+    e.uv = e.u * e.v;
+  }
   e.live = 1;
   e.cpsi = e.spsi = 0.f;
   e.ra = e.rb = 0.f;
@@ -333,6 +328,7 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
     float sum = 0.f;
     for (int i = 0; i < nS; i++) {
       const int t = (GEOM == kParallel) ? d : d * nS + i;
+      const float ft = (float)t;
       float rx, ry, invr = 1.f, cj = 1.f, sj = 0.f;
       if (GEOM == kParallel) {
         rx = sdir[i].x;
@@ -357,25 +353,29 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
       for (int k = 0; k < nElem; k++) {
         const ElemView& e = ev[k * nSub + (GEOM == kParallel ? i : 0)];
         if (!e.live) continue;
+        // integers below 2^24: (float)tcI - ft is the exact (float)(tcI - t)
+        const float ftc = (float)e.tcI;
         float rho;
         if (GEOM == kEquiangular) {
-          float x = ((float)(e.tcI - t) + e.tcF) * hdelta;
+          float x = ((ftc - ft) + e.tcF) * hdelta;
           float cf = fmaf(e.cpsi, cj, e.spsi * sj);
           rho = e.kB * cf * sin_series(x) * invr;
         } else {
-          float dt = (float)(t - e.tcI) - e.tcF;
+          float dt = (ft - ftc) - e.tcF;
           rho = e.kB * dt * invr;
         }
         // cull against the outline box's circumcircle
         float rhob = rho + (rx * e.dcby - ry * e.dcbx);
         const float arhob = fabsf(rhob);
         if (arhob > e.rbox) continue;
-        float ra, rb;
-        if (GEOM == kParallel) { ra = e.ra; rb = e.rb; }
-        else { ra = rx * e.ca + ry * e.sa; rb = -rx * e.sa + ry * e.ca; }
-        float ch = element_chord(e, rho, ra, rb);
+        float ra = 0.f, rb = 0.f;
+        if (e.type != kEllipse) {
+          if (GEOM == kParallel) { ra = e.ra; rb = e.rb; }
+          else { ra = rx * e.ca + ry * e.sa; rb = -rx * e.sa + ry * e.ca; }
+        }
+        float ch = element_chord(e, rho, rx, ry, ra, rb);
         if (ch <= 0.f) continue;
-        int bt = arhob < e.rin ? 1 : box_test(e, rho, rx, ry);
+        int bt = arhob < e.rin ? 1 : box_test(e, rhob, rx, ry);
         if (bt == 0) {
           // repeat the reference's FP64 box clip on this ray's end points
           const PElem& pe = elems[k];
