@@ -28,8 +28,12 @@ namespace ctgpu {
 namespace {
 
 struct ElemView {
+  // first 16 bytes, read together by the ray loop: rays t outside [tlo, thi]
+  // cannot reach the outline box's circumcircle (tlo > thi: no ray of this
+  // view meets the element); t_c = tcI + tcF with ftc = (float)tcI
+  int tlo, thi;
+  float ftc, tcF;
   float kB;          // rho = kB * (t - t_c)   (times 1/|r| for fan beams)
-  float tcF;         // t_c = tcI + tcF
   int tcI;
   int type;
   float ca, sa;      // element rotation
@@ -38,11 +42,11 @@ struct ElemView {
   float hx, hy, rbox;
   float cpsi, spsi;  // equiangular: cos/sin of psi'
   float ra, rb;      // parallel: ray direction in the element frame
-  int live;          // 0: no ray of this view can meet the element
   float rin;         // radius of the outline box's inscribed circle, less the margin
   // E = (ra/u)^2 + (rb/v)^2 of a unit ray direction (rx, ry) as a quadratic
   // form, E = qa rx^2 + qb rx ry + qc ry^2, and u v (ellipse chords)
   float qa, qb, qc, uv;
+  int pad0, pad1;
 };
 static_assert(sizeof(ElemView) % 16 == 0, "ElemView records keep 16-byte alignment");
 
@@ -178,6 +182,76 @@ __device__ __forceinline__ void split_root(double t, int& ti, float& tf) {
   tf = (float)(t - fl);
 }
 
+// Ray indices whose lines can come within the outline box's circumcircle
+// (centre B, radius rbox): an early-out ahead of the rays' exact test, so it
+// only has to contain them -- FP32 tangents from the source, widened by two
+// rays.  Parallel rays: |rho_B(d)| = |A - d B| <= rbox is an interval.  Fan
+// rays: the two tangents from the source to the circle, mapped to ray
+// indices (detector line or arc).  The radius is widened well past the FP32
+// rounding of the rays' own distance test (a few ulp of |rho| + |dcb|).
+template <int GEOM>
+__device__ void ray_range(const RaysumLaunch& L, const RayView& g, const PElem& pe, int sub,
+                          ElemView& e) {
+  const int kAll = 1 << 30;
+  e.tlo = -kAll;
+  e.thi = kAll;
+  const double Bx = pe.cx + (double)pe.dcbx, By = pe.cy + (double)pe.dcby;
+  const double R = 1.0001 * (double)pe.rbox + 1e-4 * (fabs(pe.dcbx) + fabs(pe.dcby)) + 1e-30;
+  double t1, t2;
+  if (GEOM == kParallel) {
+    double rx = (g.D0x + sub * g.dDx) - g.S0x, ry = (g.D0y + sub * g.dDy) - g.S0y;
+    const double inv = 1.0 / sqrt(rx * rx + ry * ry);
+    rx *= inv;
+    ry *= inv;
+    const double A = cross2(rx, ry, Bx - g.S0x, By - g.S0y), B = cross2(rx, ry, g.dSx, g.dSy);
+    if (B == 0.0) return;
+    t1 = (A - R) / B;
+    t2 = (A + R) / B;
+  } else {
+    const float wx = (float)(Bx - g.S0x), wy = (float)(By - g.S0y);
+    const float dist = sqrtf(wx * wx + wy * wy);
+    if (!(dist > 1.01f * (float)R)) return;
+    const float sb = (float)R / dist;
+    const float cb = sqrtf(1.f - sb * sb);
+    const float ux[2] = {(wx * cb - wy * sb) / dist, (wx * cb + wy * sb) / dist};
+    const float uy[2] = {(wy * cb + wx * sb) / dist, (wy * cb - wx * sb) / dist};
+    float tt[2];
+    if (GEOM == kEquilinear) {
+      // both tangents must meet the detector line on the same side
+      const float d0 = g.stx * uy[0] - g.sty * ux[0], d1 = g.stx * uy[1] - g.sty * ux[1];
+      if ((d0 > 0.f) != (d1 > 0.f)) return;
+    }
+    for (int k = 0; k < 2; k++) {
+      if (GEOM == kEquilinear) {
+        const float den = g.stx * uy[k] - g.sty * ux[k];
+        if (fabsf(den) < 1e-30f) return;
+        tt[k] = -(g.rsx * uy[k] - g.rsy * ux[k]) / den;
+      } else {
+        // far crossing of the tangent with the detector arc |p| = CD, as a
+        // ray index from its angle about the arc's middle
+        const float Sx = g.Sx, Sy = g.Sy, CD = (float)L.centerDetectorLength;
+        const float su = Sx * ux[k] + Sy * uy[k];
+        const float disc = su * su - (Sx * Sx + Sy * Sy - CD * CD);
+        if (!(disc >= 0.f)) return;
+        const float lam = -su + sqrtf(disc);
+        const float Dx = Sx + lam * ux[k], Dy = Sy + lam * uy[k];
+        const float cm = (float)g.cm, sm = (float)g.sm;
+        tt[k] = (atan2f(cm * Dy - sm * Dx, cm * Dx + sm * Dy) + (float)g.midRel) *
+                (float)g.invDelta;
+      }
+    }
+    t1 = tt[0];
+    t2 = tt[1];
+  }
+  const double pad = 2.0 + 1e-5 * (fabs(t1) + fabs(t2));
+  double lo = fmin(t1, t2) - pad, hi = fmax(t1, t2) + pad;
+  if (!(lo == lo) || !(hi == hi)) return;
+  lo = fmax(lo, -(double)kAll);
+  hi = fmin(hi, (double)kAll);
+  e.tlo = (int)floor(lo);
+  e.thi = (int)ceil(hi);
+}
+
 // FP64 set-up of one (view, element[, ray sample]) record.
 template <int GEOM>
 __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const float2* sdir,
@@ -202,16 +276,15 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
     e.qc = (float)(sn * sn * iu2 + c * c * iv2);
     e.uv = e.u * e.v;
   }
-  e.live = 1;
   e.cpsi = e.spsi = 0.f;
   e.ra = e.rb = 0.f;
   e.kB = 0.f;
   e.tcI = 0;
   e.tcF = 0.f;
-  if (pe.type < 0) {   // absent from this view (3-D phantom cross-section)
-    e.live = 0;
-    return;
-  }
+  e.ftc = 0.f;
+  e.tlo = 1;   // no ray until ray_range below
+  e.thi = 0;
+  if (pe.type < 0) return;   // absent from this view (3-D phantom cross-section)
   if (GEOM == kParallel) {
     // ray direction of sub-sample `sub` (independent of the detector index)
     double rx = (g.D0x + sub * g.dDx) - g.S0x, ry = (g.D0y + sub * g.dDy) - g.S0y;
@@ -221,7 +294,7 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
     double wx = pe.cx - g.S0x, wy = pe.cy - g.S0y;
     double A = cross2(rx, ry, wx, wy), B = cross2(rx, ry, g.dSx, g.dSy);
     // rho(d) = A - d B
-    if (B == 0.0) { e.live = 0; return; }
+    if (B == 0.0) return;
     split_root(A / B, e.tcI, e.tcF);
     e.kB = (float)(-B);
     e.ra = (float)(rx * pe.cosr + ry * pe.sinr);
@@ -230,7 +303,7 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
     double wx = pe.cx - g.S0x, wy = pe.cy - g.S0y;
     double A = cross2(g.D0x - g.S0x, g.D0y - g.S0y, wx, wy);
     double B = cross2(g.dDx, g.dDy, wx, wy);
-    if (B == 0.0) { e.live = 0; return; }
+    if (B == 0.0) return;
     split_root(-A / B, e.tcI, e.tcF);
     e.kB = (float)B;
   } else {
@@ -245,7 +318,7 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
     const double wx = pe.cx - g.S0x, wy = pe.cy - g.S0y;
     const double wn = sqrt(wx * wx + wy * wy);
     const double q = cross2(g.S0x, g.S0y, wx, wy) / (CD * wn);
-    if (!(fabs(q) <= 1.0)) { e.live = 0; return; }
+    if (!(fabs(q) <= 1.0)) return;
     const double cb = sqrt((1.0 - q) * (1.0 + q));
     const double iw = 1.0 / wn;
     const double u1x = (wx * cb + wy * q) * iw, u1y = (wy * cb - wx * q) * iw;
@@ -263,6 +336,8 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
     e.cpsi = cp;
     e.spsi = sp;
   }
+  e.ftc = (float)e.tcI;
+  ray_range<GEOM>(L, g, pe, sub, e);
 }
 
 }  // namespace
@@ -352,16 +427,17 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
       }
       for (int k = 0; k < nElem; k++) {
         const ElemView& e = ev[k * nSub + (GEOM == kParallel ? i : 0)];
-        if (!e.live) continue;
+        const int4 hdr = *reinterpret_cast<const int4*>(&e);
+        if (t < hdr.x || t > hdr.y) continue;
         // integers below 2^24: (float)tcI - ft is the exact (float)(tcI - t)
-        const float ftc = (float)e.tcI;
+        const float ftc = __int_as_float(hdr.z), tcF = __int_as_float(hdr.w);
         float rho;
         if (GEOM == kEquiangular) {
-          float x = ((ftc - ft) + e.tcF) * hdelta;
+          float x = ((ftc - ft) + tcF) * hdelta;
           float cf = fmaf(e.cpsi, cj, e.spsi * sj);
           rho = e.kB * cf * sin_series(x) * invr;
         } else {
-          float dt = (ft - ftc) - e.tcF;
+          float dt = (ft - ftc) - tcF;
           rho = e.kB * dt * invr;
         }
         // cull against the outline box's circumcircle
