@@ -47,6 +47,28 @@ class BatchProblem(C.Structure):
                 ("h_view_angles", C.c_void_p), ("d_image", C.c_void_p)]
 
 
+class PjInfo(C.Structure):
+    """ctgpu_pj_info: a .pj header"""
+    _fields_ = [("geometry", Geometry), ("calc_time", C.c_double), ("date", C.c_int32 * 6),
+                ("header_size", C.c_int32), ("remark_length", C.c_int32)]
+
+
+class IfInfo(C.Structure):
+    """ctgpu_if_info: an .if header"""
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("pixel_format", C.c_int32),
+                ("pixel_size", C.c_int32), ("data_type", C.c_int32), ("n_labels", C.c_int32),
+                ("increment_known", C.c_int32), ("extent_known", C.c_int32),
+                ("increment", C.c_double * 2), ("extent", C.c_double * 4),
+                ("offset_pv", C.c_double), ("scale_pv", C.c_double),
+                ("header_size", C.c_int32), ("reserved", C.c_int32)]
+
+
+class IfLabel(C.Structure):
+    """ctgpu_if_label"""
+    _fields_ = [("type", C.c_int32), ("date", C.c_int32 * 6), ("calc_time", C.c_double),
+                ("text", C.c_char_p), ("text_length", C.c_int32), ("reserved", C.c_int32)]
+
+
 BATCH_AUTOTUNE = 1
 BATCH_GRAPH = 2
 
@@ -106,6 +128,16 @@ SIGNATURES = {
     "ctgpu_batch_run": ([_p, _p], _i),
     "ctgpu_batch_shape": ([_p, C.POINTER(_i), C.POINTER(_i)], _i),
     "ctgpu_batch_destroy": ([_p], None),
+    "ctgpu_pj_read_header": ([_s, C.POINTER(PjInfo), _s, _i], _i),
+    "ctgpu_pj_read_device": ([_s, _p, _i, _p, C.POINTER(_i), _p], _i),
+    "ctgpu_pj_write_device": ([_s, C.POINTER(PjInfo), _s, _p, _i, _p, _p], _i),
+    "ctgpu_if_read_header": ([_s, C.POINTER(IfInfo)], _i),
+    "ctgpu_if_read_labels": ([_s, C.POINTER(IfLabel), _i, _s, C.c_size_t, C.POINTER(_i)], _i),
+    "ctgpu_if_read_device": ([_s, _p, _p], _i),
+    "ctgpu_if_write_device": ([_s, C.POINTER(IfInfo), C.POINTER(IfLabel), _i, _p, _p], _i),
+    "ctgpu_sino_to_image": ([_p, _i, _i, _i, _p, _p], _i),
+    "ctgpu_image_compare": ([_p, _p, _i, _i, _i, C.c_size_t, _p, _p], _i),
+    "ctgpu_image_arith": ([_s, _p, _p, _p, C.c_size_t, _p], _i),
     "ctgpu_backproject_diff_noalloc": ([C.POINTER(Geometry), _i, _i, _s, C.POINTER(Roi), _p, _i,
                                         _p, _i, _p, _i, _p], _i),
 }

@@ -35,7 +35,8 @@ FILE_FLAGS = {"k_helical.cu": ["--fmad=false"]}
 EXTRA_FLAGS = os.environ.get("CTGPU_NVCC_FLAGS", "").split()
 
 LIB_SOURCES = ["k_common.cu", "k_raysum.cu", "k_filter.cu", "k_backproject.cu", "k_helical.cu",
-               "ctgpu_api.cpp", "filter_design.cpp", "ctsim_api.cpp", "k_noalloc.cu", "k_rebin.cu"]
+               "ctgpu_api.cpp", "filter_design.cpp", "ctsim_api.cpp", "k_noalloc.cu", "k_rebin.cu",
+               "k_fileio.cu", "ctgpu_io.cpp"]
 TOOL_SOURCES = ["tools/ctsimtext.cpp"]
 
 

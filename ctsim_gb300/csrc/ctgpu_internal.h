@@ -242,4 +242,33 @@ cudaError_t launch_project_table(const BackprojLaunch& L, const float* image, fl
 cudaError_t launch_helical180li(const HelicalLaunch& L, cudaStream_t s);
 cudaError_t launch_halfscan_feather(const HelicalLaunch& L, cudaStream_t s);
 
+// ----- file formats and image utilities (k_fileio.cu) ----------------------
+// .pj view records: f64 angle, u32 nDet, nDet x f32, as 3 + nDet 32-bit words
+cudaError_t launch_pj_pack(const float* sino, int pitch, const double* angles, int nViews,
+                           int nDet, uint32_t* out, cudaStream_t s);
+// status[0] += records whose nDet word differs from nDet, status[1] = min view
+cudaError_t launch_pj_unpack(const uint32_t* in, int nViews, int nDet, float* sino, int pitch,
+                             double* angles, int viewOffset, unsigned int* status,
+                             cudaStream_t s);
+// pj2if: image[ix][iy] (nDet x nView, column-major) = sino[nView - 1 - iy][ix]
+cudaError_t launch_sino_to_image(const float* sino, int pitch, int nView, int nDet, float* image,
+                                 cudaStream_t s);
+cudaError_t launch_f64_to_f32(const double* in, float* out, size_t n, cudaStream_t s);
+// op 0 add, 1 subtract, 2 multiply, 3 divide (FP32)
+cudaError_t launch_image_arith(int op, const float* a, const float* b, float* out, size_t n,
+                               cudaStream_t s);
+// comparative statistics of image pairs: part holds nImages x compare_blocks(nx, ny)
+// x kCmpParts doubles, out nImages x (d, r, e)
+constexpr int kCmpParts = 6;
+struct CompareLaunch {
+  const float* a;
+  const float* b;
+  size_t strideA, strideB;   // floats between images
+  int nx, ny, nImages;
+  double* part;
+  double* out;
+};
+int compare_blocks(int nx, int ny);
+cudaError_t launch_image_compare(const CompareLaunch& L, cudaStream_t s);
+
 }  // namespace ctgpu

@@ -1,7 +1,10 @@
-// ctsimtext.cpp -- the phm2pj, pjrec, pjHinterp and pjinfo command-line tools on
-// the GPU library, with the reference's option tables, defaults, file formats
-// and exit codes (tools/phm2pj.cpp:33-393, tools/pjrec.cpp:31-366,
-// tools/pjHinterp.cpp:32-149, tools/ctsimtext.cpp:239-280).  Invoked as
+// ctsimtext.cpp -- the phm2pj, pjrec, pjHinterp, pjinfo, phm2if, pj2if and if2
+// command-line tools on the GPU library, with the reference's option tables,
+// defaults, file formats and exit codes (tools/phm2pj.cpp:33-393,
+// tools/pjrec.cpp:31-366, tools/pjHinterp.cpp:32-149, tools/phm2if.cpp,
+// tools/pj2if.cpp:33-133, tools/if2.cpp:33-307, tools/ctsimtext.cpp:239-280).
+// pj2if and if2 keep the data on the device between the file reads and
+// writes (ctgpu_pj_read_device / ctgpu_if_read_device ... _write_device).  Invoked as
 // `ctgpu_ctsimtext <function> args...` or through a link named after the
 // function.
 #include <getopt.h>
@@ -14,6 +17,9 @@
 #include <sstream>
 #include <string>
 #include <strings.h>
+#include <vector>
+
+#include <cuda_runtime.h>
 
 #include "../../../include/ctsim_gpu.h"
 
@@ -451,6 +457,252 @@ int pjinfo_main(int argc, char* const argv[]) {
   return 0;
 }
 
+// ------------------------------------------------------------------- pj2if --
+// device buffers freed on exit
+struct DeviceBuffers {
+  std::vector<void*> p;
+  void* get(size_t bytes) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, bytes ? bytes : 1) != cudaSuccess) return nullptr;
+    p.push_back(q);
+    return q;
+  }
+  ~DeviceBuffers() {
+    for (void* q : p) cudaFree(q);
+  }
+};
+
+void pj2if_usage(const char* program) {
+  std::cout << "usage: " << base_name(program) << " in-proj-file out-if-file [OPTIONS]\n";
+  std::cout << "Converts a projection file to a imagefile\n\n";
+  std::cout << "   --polar     Convert to polar format\n";
+  std::cout << "   --verbose   Verbose mode\n";
+  std::cout << "   --version   Print version\n";
+  std::cout << "   --help      Print this help message\n";
+}
+
+int pj2if_main(int argc, char* const argv[]) {
+  enum { O_VERBOSE, O_HELP, O_VERSION, O_POLAR };
+  const struct option options[] = {{"polar", 0, 0, O_POLAR},     {"verbose", 0, 0, O_VERBOSE},
+                                   {"help", 0, 0, O_HELP},       {"version", 0, 0, O_VERSION},
+                                   {0, 0, 0, 0}};
+  bool verbose = false;
+  optind = 0;
+  auto t0 = std::chrono::steady_clock::now();
+  while (1) {
+    int c = getopt_long(argc, argv, "", options, nullptr);
+    if (c == -1) break;
+    switch (c) {
+      case O_VERBOSE: verbose = true; break;
+      case O_POLAR: break;   // accepted and unused, as in the reference
+      case O_VERSION: std::cout << "Version 5.2.0 (GB300)" << std::endl; return 0;
+      case O_HELP: case '?': pj2if_usage(argv[0]); return 0;
+      default: pj2if_usage(argv[0]); return 1;
+    }
+  }
+  if (argc - optind != 2) { pj2if_usage(argv[0]); return 1; }
+  const char* pjName = argv[optind];
+  const char* imName = argv[optind + 1];
+  ctgpu_pj_info info;
+  std::vector<char> remark(65536);
+  if (ctgpu_pj_read_header(pjName, &info, remark.data(), (int)remark.size()) != CTGPU_OK) {
+    std::cerr << "Can not open projection file " << pjName << std::endl;
+    return 1;
+  }
+  if (verbose) {
+    Projections pj;
+    if (pj.read(pjName)) {
+      std::string s;
+      pj.printScanInfo(s);
+      std::cout << s;
+    }
+  }
+  const int nView = info.geometry.n_view, nDet = info.geometry.n_det;
+  const int pitch = (nDet + 3) & ~3;
+  DeviceBuffers mem;
+  float* dSino = static_cast<float*>(mem.get(sizeof(float) * (size_t)nView * pitch));
+  double* dAngles = static_cast<double*>(mem.get(sizeof(double) * (size_t)nView));
+  float* dImage = static_cast<float*>(mem.get(sizeof(float) * (size_t)nView * nDet));
+  if (!dSino || !dAngles || !dImage) {
+    std::cerr << "out of device memory\n";
+    return 1;
+  }
+  if (ctgpu_pj_read_device(pjName, dSino, pitch, dAngles, nullptr, nullptr) != CTGPU_OK ||
+      ctgpu_sino_to_image(dSino, pitch, nView, nDet, dImage, nullptr) != CTGPU_OK) {
+    std::cerr << ctgpu_last_error() << std::endl;
+    return 1;
+  }
+  ctgpu_if_info out;
+  std::memset(&out, 0, sizeof(out));
+  out.nx = nDet;
+  out.ny = nView;
+  out.scale_pv = 1.0;
+  // the projections' label (projections.cpp:631-634), then the conversion
+  ctgpu_if_label labels[2];
+  std::memset(labels, 0, sizeof(labels));
+  labels[0].type = 1;
+  std::memcpy(labels[0].date, info.date, sizeof(info.date));
+  labels[0].calc_time = info.calc_time;
+  labels[0].text = remark.data();
+  labels[0].text_length = info.remark_length;
+  labels[1].type = 1;
+  labels[1].text = "Conversion from .pj to .if";
+  labels[1].calc_time = seconds_since(t0);
+  if (ctgpu_if_write_device(imName, &out, labels, 2, dImage, nullptr) != CTGPU_OK) {
+    std::cerr << ctgpu_last_error() << std::endl;
+    return 1;
+  }
+  return 0;
+}
+
+// --------------------------------------------------------------------- if2 --
+void if2_usage(const char* program) {
+  std::cout << "usage: " << base_name(program) << " infile1 infile2 outfile [OPTIONS]\n";
+  std::cout << "Perform functions on two input image files\n\n";
+  std::cout << "     infile1            Name of first input IF file\n";
+  std::cout << "     infile2            Name of second input IF file\n";
+  std::cout << "     outfile            Name of output Image or Plot file\n";
+  std::cout << "     --add              Add images\n";
+  std::cout << "     --sub              Subtract image 2 from image 1\n";
+  std::cout << "     --mul              Multiply images\n";
+  std::cout << "     --comp             Compare images\n";
+  std::cout << "     --column-plot n    Plot column\n";
+  std::cout << "     --row-plot n       Plot row\n";
+  std::cout << "     --verbose          Verbose modem\n";
+  std::cout << "     --version          Print version\n";
+  std::cout << "     --help             Print this help message\n";
+}
+
+// an .if file's labels, with `prefix` before each text (Array2dFile::labelsCopy)
+bool copy_labels(const char* fn, const char* prefix, std::vector<std::string>& texts,
+                 std::vector<ctgpu_if_label>& out) {
+  ctgpu_if_info info;
+  if (ctgpu_if_read_header(fn, &info) != CTGPU_OK) return false;
+  std::vector<ctgpu_if_label> l(info.n_labels > 0 ? info.n_labels : 1);
+  std::vector<char> buf((size_t)info.n_labels * 65536 + 1);
+  int n = 0;
+  if (ctgpu_if_read_labels(fn, l.data(), info.n_labels, buf.data(), buf.size(), &n) != CTGPU_OK)
+    return false;
+  for (int i = 0; i < n && i < info.n_labels; i++) {
+    texts.push_back(std::string(prefix) + (l[i].text ? l[i].text : ""));
+    out.push_back(l[i]);
+  }
+  return true;
+}
+
+int if2_main(int argc, char* const argv[]) {
+  enum { O_ADD, O_SUB, O_MUL, O_DIVIDE, O_COMP, O_ROW_PLOT, O_COLUMN_PLOT, O_VERBOSE, O_HELP,
+         O_VERSION };
+  const struct option options[] = {
+      {"add", 0, 0, O_ADD},          {"sub", 0, 0, O_SUB},
+      {"multiply", 0, 0, O_MUL},     {"divide", 0, 0, O_DIVIDE},
+      {"comp", 0, 0, O_COMP},        {"column-plot", 1, 0, O_COLUMN_PLOT},
+      {"row-plot", 1, 0, O_ROW_PLOT}, {"verbose", 0, 0, O_VERBOSE},
+      {"help", 0, 0, O_HELP},        {"version", 0, 0, O_VERSION},
+      {0, 0, 0, 0}};
+  const char* op = nullptr;
+  std::string opTitle;
+  bool comp = false, imageOut = false, plotOut = false;
+  optind = 0;
+  auto t0 = std::chrono::steady_clock::now();
+  while (1) {
+    int c = getopt_long(argc, argv, "", options, nullptr);
+    if (c == -1) break;
+    switch (c) {
+      case O_ADD: op = "add"; opTitle = "Add Images"; imageOut = true; break;
+      case O_SUB: op = "subtract"; opTitle = "Subtract Images"; imageOut = true; break;
+      case O_MUL: op = "multiply"; opTitle = "Multiply Images"; imageOut = true; break;
+      case O_DIVIDE: op = "divide"; opTitle = "Divide Images"; imageOut = true; break;
+      case O_ROW_PLOT: case O_COLUMN_PLOT: {
+        int v;
+        if (!parse_int(optarg, v)) if2_usage(argv[0]);
+        plotOut = true;
+        break;
+      }
+      case O_COMP: comp = true; break;
+      case O_VERBOSE: break;
+      case O_VERSION: std::cout << "Version 5.2.0 (GB300)" << std::endl; return 0;
+      case O_HELP: case '?': if2_usage(argv[0]); return 0;
+      default: if2_usage(argv[0]); return 1;
+    }
+  }
+  if ((imageOut || plotOut) && optind + 3 != argc) { if2_usage(argv[0]); return 1; }
+  if (!(imageOut || plotOut) && optind + 2 != argc) { if2_usage(argv[0]); return 1; }
+  const char* in1 = argv[optind];
+  const char* in2 = argv[optind + 1];
+  ctgpu_if_info h1, h2;
+  if (ctgpu_if_read_header(in1, &h1) != CTGPU_OK || ctgpu_if_read_header(in2, &h2) != CTGPU_OK) {
+    std::cerr << "Error reading an image" << std::endl;
+    return 1;
+  }
+  if (h1.nx != h2.nx || h1.ny != h2.ny) {
+    std::cerr << "Error: Size of image 1 (" << h1.nx << "," << h1.ny << ") and image 2 ("
+              << h2.nx << "," << h2.ny << ") do not match" << std::endl;
+    return 1;
+  }
+  if (imageOut && plotOut) {
+    std::cerr << "Both Image and Plot output files can not be selected simultaneously" << std::endl;
+    return 1;
+  }
+  if (plotOut) {
+    std::cerr << "if2: plot output files are not part of this library" << std::endl;
+    return 1;
+  }
+  const size_t n = (size_t)h1.nx * h1.ny;
+  DeviceBuffers mem;
+  float* dA = static_cast<float*>(mem.get(sizeof(float) * n));
+  float* dB = static_cast<float*>(mem.get(sizeof(float) * n));
+  float* dOut = imageOut ? static_cast<float*>(mem.get(sizeof(float) * n)) : nullptr;
+  if (!dA || !dB || (imageOut && !dOut)) {
+    std::cerr << "out of device memory\n";
+    return 1;
+  }
+  if (ctgpu_if_read_device(in1, dA, nullptr) != CTGPU_OK ||
+      ctgpu_if_read_device(in2, dB, nullptr) != CTGPU_OK) {
+    std::cerr << "Error reading an image: " << ctgpu_last_error() << std::endl;
+    return 1;
+  }
+  if (op && ctgpu_image_arith(op, dA, dB, dOut, n, nullptr) != CTGPU_OK) {
+    std::cerr << ctgpu_last_error() << std::endl;
+    return 1;
+  }
+  if (comp) {
+    double dre[3];
+    if (ctgpu_image_compare(dA, dB, 1, h1.nx, h1.ny, n, dre, nullptr) != CTGPU_OK) {
+      std::cerr << ctgpu_last_error() << std::endl;
+      return 1;
+    }
+    std::cout << "d=" << dre[0] << ", r=" << dre[1] << ", e=" << dre[2] << std::endl;
+  }
+  if (imageOut) {
+    std::vector<std::string> texts;
+    std::vector<ctgpu_if_label> labels;
+    copy_labels(in1, "if2 file 1: ", texts, labels);
+    copy_labels(in2, "if2 file 2: ", texts, labels);
+    texts.push_back(opTitle);
+    ctgpu_if_label last;
+    std::memset(&last, 0, sizeof(last));
+    last.type = 1;
+    last.calc_time = seconds_since(t0);
+    labels.push_back(last);
+    for (size_t i = 0; i < labels.size(); i++) {
+      labels[i].text = texts[i].c_str();
+      labels[i].text_length = (int32_t)texts[i].size();
+    }
+    ctgpu_if_info out;
+    std::memset(&out, 0, sizeof(out));
+    out.nx = h1.nx;
+    out.ny = h1.ny;
+    out.scale_pv = 1.0;
+    if (ctgpu_if_write_device(argv[optind + 2], &out, labels.data(), (int)labels.size(), dOut,
+                              nullptr) != CTGPU_OK) {
+      std::cerr << ctgpu_last_error() << std::endl;
+      return 1;
+    }
+  }
+  return 0;
+}
+
 int dispatch(int argc, char* argv[]) {
   const char* f = base_name(argv[0]);
   if (!strcasecmp(f, "phm2pj")) return phm2pj_main(argc, argv);
@@ -458,8 +710,10 @@ int dispatch(int argc, char* argv[]) {
   if (!strcasecmp(f, "pjHinterp")) return pjHinterp_main(argc, argv);
   if (!strcasecmp(f, "pjinfo")) return pjinfo_main(argc, argv);
   if (!strcasecmp(f, "phm2if")) return phm2if_main(argc, argv);
+  if (!strcasecmp(f, "pj2if")) return pj2if_main(argc, argv);
+  if (!strcasecmp(f, "if2")) return if2_main(argc, argv);
   std::cout << "Unknown function name: " << f << "\n"
-            << "usage: ctgpu_ctsimtext phm2pj|pjrec|pjHinterp|pjinfo|phm2if args...\n";
+            << "usage: ctgpu_ctsimtext phm2pj|pjrec|pjHinterp|pjinfo|phm2if|pj2if|if2 args...\n";
   return 1;
 }
 

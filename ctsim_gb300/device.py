@@ -9,7 +9,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import Geometry, Roi, RUN_ACCUMULATE, RUN_POSTPROCESS, check, enc, lib
+from ._lib import (Geometry, IfInfo, IfLabel, PjInfo, Roi, RUN_ACCUMULATE, RUN_POSTPROCESS,
+                   check, enc, lib)
 
 
 def _torch():
@@ -26,6 +27,12 @@ def stream_handle(stream=None):
 def _ptr(t):
     if not t.is_cuda or not t.is_contiguous() or t.dtype != _torch().float32:
         raise ValueError("expected a contiguous float32 CUDA tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def _ptrd(t):
+    if not t.is_cuda or not t.is_contiguous() or t.dtype != _torch().float64:
+        raise ValueError("expected a contiguous float64 CUDA tensor")
     return C.c_void_p(t.data_ptr())
 
 
@@ -340,3 +347,120 @@ def halfscan_feather_host(geometry, data):
     from . import sync
     sync()
     return t[:, :data.shape[1]].cpu().numpy()
+
+
+# ---------------------------------------------------------------- file I/O --
+def read_pj_header(path):
+    """ctgpu_pj_read_header: (PjInfo, remark)."""
+    info = PjInfo()
+    buf = C.create_string_buffer(65536)
+    check(lib().ctgpu_pj_read_header(enc(str(path)), C.byref(info), buf, len(buf)))
+    return info, buf.value.decode("latin-1")
+
+
+def read_pj(path, device="cuda", stream=None):
+    """A .pj file straight into device memory (ctgpu_pj_read_device): returns
+    (PjInfo, remark, sino [n_view, pitch] FP32 tensor, angles [n_view] FP64
+    tensor, views read)."""
+    torch = _torch()
+    info, remark = read_pj_header(path)
+    g = info.geometry
+    sino = torch.empty((g.n_view, pitch_for(g.n_det)), dtype=torch.float32, device=device)
+    ang = torch.empty((g.n_view,), dtype=torch.float64, device=device)
+    n = C.c_int()
+    check(lib().ctgpu_pj_read_device(enc(str(path)), _ptr(sino), sino.shape[1], _ptrd(ang),
+                                     C.byref(n), stream_handle(stream)))
+    return info, remark, sino, ang, n.value
+
+
+def write_pj(path, info, remark, sino, angles, stream=None):
+    """ctgpu_pj_write_device: sino [n_view, pitch] and angles (FP64) on the device."""
+    check(lib().ctgpu_pj_write_device(enc(str(path)), C.byref(info), enc(remark or ""),
+                                      _ptr(sino), sino.shape[1], _ptrd(angles),
+                                      stream_handle(stream)))
+
+
+def read_if_header(path):
+    info = IfInfo()
+    check(lib().ctgpu_if_read_header(enc(str(path)), C.byref(info)))
+    return info
+
+
+def read_if_labels(path):
+    """[(type, text, calc_time, date)] of an .if file."""
+    info = read_if_header(path)
+    n = info.n_labels
+    labels = (IfLabel * max(n, 1))()
+    text = C.create_string_buffer(n * 65536 + 1)
+    got = C.c_int()
+    check(lib().ctgpu_if_read_labels(enc(str(path)), labels, n, text, len(text), C.byref(got)))
+    return [(l.type, (l.text or b"").decode("latin-1"), l.calc_time, tuple(l.date))
+            for l in labels[:got.value]]
+
+
+def read_if(path, device="cuda", stream=None):
+    """An .if file's real pixels into a device FP32 tensor [nx, ny]
+    (ctgpu_if_read_device): returns (IfInfo, image)."""
+    torch = _torch()
+    info = read_if_header(path)
+    im = torch.empty((info.nx, info.ny), dtype=torch.float32, device=device)
+    check(lib().ctgpu_if_read_device(enc(str(path)), _ptr(im), stream_handle(stream)))
+    return info, im
+
+
+def write_if(path, image, info=None, labels=(), stream=None):
+    """ctgpu_if_write_device: image [nx, ny] FP32 on the device; labels as
+    (type, text, calc_time[, date])."""
+    if info is None:
+        info = IfInfo()
+        info.scale_pv = 1.0
+    info.nx, info.ny = image.shape
+    arr = (IfLabel * max(len(labels), 1))()
+    keep = []
+    for k, l in enumerate(labels):
+        b = l[1].encode("latin-1")
+        keep.append(b)
+        arr[k].type = l[0]
+        arr[k].text = b
+        arr[k].text_length = len(b)
+        arr[k].calc_time = l[2]
+        if len(l) > 3:
+            arr[k].date[:] = list(l[3])
+    check(lib().ctgpu_if_write_device(enc(str(path)), C.byref(info), arr, len(labels),
+                                      _ptr(image), stream_handle(stream)))
+
+
+def sino_to_image(sino, n_det, out=None, stream=None):
+    """pj2if: image [n_det, n_view] with v[ix][iy] = sino[n_view - 1 - iy][ix]."""
+    torch = _torch()
+    nv = sino.shape[0]
+    if out is None:
+        out = torch.empty((n_det, nv), dtype=torch.float32, device=sino.device)
+    check(lib().ctgpu_sino_to_image(_ptr(sino), sino.shape[1], nv, n_det, _ptr(out),
+                                    stream_handle(stream)))
+    return out
+
+
+def image_compare(a, b, stream=None):
+    """ImageFile::comparativeStatistics of device images a, b: [nx, ny] ->
+    (d, r, e), or [n, nx, ny] -> array [n, 3]."""
+    batched = a.dim() == 3
+    if not batched:
+        a, b = a.unsqueeze(0), b.unsqueeze(0)
+    assert a.shape == b.shape and a.is_contiguous() and b.is_contiguous()
+    n, nx, ny = a.shape
+    out = np.zeros((n, 3), np.float64)
+    check(lib().ctgpu_image_compare(_ptr(a), _ptr(b), n, nx, ny, nx * ny,
+                                    out.ctypes.data_as(C.c_void_p), stream_handle(stream)))
+    return out if batched else tuple(out[0])
+
+
+def image_arith(op, a, b, out=None, stream=None):
+    """ImageFile add / subtract / multiply / divide of device FP32 images."""
+    torch = _torch()
+    assert a.shape == b.shape and a.is_contiguous() and b.is_contiguous()
+    if out is None:
+        out = torch.empty_like(a)
+    check(lib().ctgpu_image_arith(enc(op), _ptr(a), _ptr(b), _ptr(out), a.numel(),
+                                  stream_handle(stream)))
+    return out

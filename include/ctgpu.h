@@ -29,6 +29,7 @@
 #ifndef CTGPU_H
 #define CTGPU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -331,6 +332,96 @@ int ctgpu_helical_plan_run(ctgpu_helical_plan* p, const float* d_in, int in_pitc
                            const int* h_interp_views, int n_slices, float* d_out, int out_pitch,
                            long long out_slice_stride, double* h_out_angles, void* stream);
 void ctgpu_helical_plan_destroy(ctgpu_helical_plan* p);
+
+/* ------------------------------------------------------------------------ */
+/* Files on device-resident data -- .pj / .if I/O (libctsim/projections.cpp: */
+/* 485-889, libctsim/array2dfile.cpp:399-640) and the pj2if / if2 utilities  */
+/* (tools/pj2if.cpp, tools/if2.cpp, libctsim/imagefile.cpp:186-528).  The    */
+/* *_device calls stream the file through page-locked buffers and return     */
+/* once the data is in place (they synchronise `stream`).                    */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  ctgpu_geometry geometry;   /* n_view, n_det, geometry and the scan fields */
+  double calc_time;
+  int32_t date[6];           /* year, month, day, hour, minute, second */
+  int32_t header_size;       /* bytes before the first view record */
+  int32_t remark_length;
+} ctgpu_pj_info;
+
+/* Projections::read's header part (projections.cpp:553-640): the fields and
+ * the remark (NUL-terminated, cut to remark_capacity - 1 bytes; may be NULL). */
+int ctgpu_pj_read_header(const char* filename, ctgpu_pj_info* info, char* remark,
+                         int remark_capacity);
+/* Projections::read's view records (detarrayRead, projections.cpp:811-843)
+ * straight into d_sino [n_view][pitch] (pad columns zeroed) and d_angles
+ * [n_view].  A file that ends early keeps the whole records it has, like the
+ * reference, the rest are zeroed, and *n_views_read (may be NULL) says how
+ * many were read.  A record whose detector count differs from the header's
+ * fails with CTGPU_ERR_IO (the reference would read past the row). */
+int ctgpu_pj_read_device(const char* filename, float* d_sino, int pitch, double* d_angles,
+                         int* n_views_read, void* stream);
+/* Projections::write (projections.cpp:780-889) from d_sino [n_view][pitch]
+ * and d_angles: header from info (header_size and remark_length are derived)
+ * and remark; byte-identical to the reference's file for the same values. */
+int ctgpu_pj_write_device(const char* filename, const ctgpu_pj_info* info, const char* remark,
+                          const float* d_sino, int pitch, const double* d_angles, void* stream);
+
+typedef struct {
+  int32_t nx, ny;
+  int32_t pixel_format;      /* 7 FP32, 8 FP64 (include/array2dfile.h:118-127) */
+  int32_t pixel_size;        /* bytes: 4 or 8 */
+  int32_t data_type;         /* 1 real, 2 complex */
+  int32_t n_labels;
+  int32_t increment_known, extent_known;
+  double increment[2];       /* x, y */
+  double extent[4];          /* xmin, xmax, ymin, ymax */
+  double offset_pv, scale_pv;
+  int32_t header_size;
+  int32_t reserved;
+} ctgpu_if_info;
+
+typedef struct {
+  int32_t type;              /* 1 history, 2 user (include/array2dfile.h:49-51) */
+  int32_t date[6];           /* all zero on writing: the current local time */
+  double calc_time;
+  const char* text;
+  int32_t text_length;       /* <= 0 on writing: strlen(text) */
+  int32_t reserved;
+} ctgpu_if_label;
+
+/* Array2dFile::headerRead (array2dfile.cpp:399-439) */
+int ctgpu_if_read_header(const char* filename, ctgpu_if_info* info);
+/* Array2dFile::labelsRead (array2dfile.cpp:559-595): up to `capacity` labels,
+ * their texts NUL-terminated in `text` (label.text NULL where it is full);
+ * *n_labels = the labels in the file. */
+int ctgpu_if_read_labels(const char* filename, ctgpu_if_label* labels, int capacity, char* text,
+                         size_t text_capacity, int* n_labels);
+/* Array2dFile::arrayDataRead (array2dfile.cpp:511-549): the real pixels,
+ * column-major, into d_image [nx][ny] as FP32 (FP64 files are converted on
+ * the device); other pixel formats return CTGPU_ERR_UNSUPPORTED. */
+int ctgpu_if_read_device(const char* filename, float* d_image, void* stream);
+/* Array2dFile::fileWrite (array2dfile.cpp:443-509, :598-640) of the FP32 real
+ * image d_image [nx][ny] with info's axes and the labels given. */
+int ctgpu_if_write_device(const char* filename, const ctgpu_if_info* info,
+                          const ctgpu_if_label* labels, int n_labels, const float* d_image,
+                          void* stream);
+/* pj2if (tools/pj2if.cpp:118-125): d_image [n_det][n_view] column-major with
+ * v[ix][iy] = row n_view - 1 - iy, detector ix of d_sino [n_view][pitch]. */
+int ctgpu_sino_to_image(const float* d_sino, int pitch, int n_view, int n_det, float* d_image,
+                        void* stream);
+/* ImageFile::comparativeStatistics (imagefile.cpp:186-240), what if2 --comp
+ * prints, for n_images pairs (d_a + i * image_stride, d_b + i * image_stride)
+ * of nx x ny images: h_dre[3 i ..] = d, r, e.  e is exact; d and r agree with
+ * the reference's sequential FP64 sums to about 1e-12 relative and do not
+ * depend on timing.  An image smaller than 2 x 2 gives e = -1 as there. */
+int ctgpu_image_compare(const float* d_a, const float* d_b, int n_images, int nx, int ny,
+                        size_t image_stride, double* h_dre, void* stream);
+/* ImageFile::addImages / subtractImages / multiplyImages / divideImages
+ * (imagefile.cpp:378-528) on real FP32 images: op "add" | "subtract" |
+ * "multiply" | "divide"; d_out[i] = d_a[i] op d_b[i] for n pixels.  Division
+ * by zero gives inf / nan, as the reference (its zero test is on a pointer). */
+int ctgpu_image_arith(const char* op, const float* d_a, const float* d_b, float* d_out, size_t n,
+                      void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Allocation-free variant                                                   */

@@ -1671,3 +1671,40 @@ int ora_project_image(const ora_geom* g, const double* image, int nx, int ny,
   }
   return 1;
 }
+
+/* ---- ImageFile::comparativeStatistics (libctsim/imagefile.cpp:186-240) ----
+ * FP32 images [nx][ny] (column-major, v[ix][iy]); the differences and the
+ * 2x2 block sums are FP32 expressions there, the sums FP64, in this order. */
+int ora_image_compare(const float* a, const float* b, int nx, int ny, double out[3]) {
+  if (nx <= 0 || ny <= 0) return 0;
+  double mean = 0.;
+  for (int ix = 0; ix < nx; ix++)
+    for (int iy = 0; iy < ny; iy++) mean += a[(size_t)ix * ny + iy];
+  mean /= (unsigned int)nx * (unsigned int)ny;
+  double sqErr = 0., absErr = 0., sqDev = 0., absVal = 0.;
+  for (int ix = 0; ix < nx; ix++)
+    for (int iy = 0; iy < ny; iy++) {
+      const size_t i = (size_t)ix * ny + iy;
+      const float fd = a[i] - b[i];
+      const double diff = fd;
+      sqErr += diff * diff;
+      absErr += fabs(diff);
+      const double dm = a[i] - mean;
+      sqDev += dm * dm;
+      absVal += fabs((double)a[i]);
+    }
+  out[0] = sqrt(sqErr / sqDev);
+  out[1] = absErr / absVal;
+  const int hx = nx / 2, hy = ny / 2;
+  double eMax = -1;
+  for (int i3 = 0; i3 < hx; i3++)
+    for (int iy = 0; iy < hy; iy++) {
+      const size_t o0 = (size_t)(2 * i3) * ny + 2 * iy, o1 = o0 + ny;
+      const float sa = a[o0] + a[o1] + a[o0 + 1] + a[o1 + 1];
+      const float sb = b[o0] + b[o1] + b[o0 + 1] + b[o1 + 1];
+      const double err = fabs(0.25 * sa - 0.25 * sb);
+      if (err > eMax) eMax = err;
+    }
+  out[2] = eMax;
+  return 1;
+}

@@ -143,6 +143,9 @@ void ora_phantom_to_image(const ora_phantom* p, int nx, int ny, double viewRatio
 int  ora_project_image(const ora_geom* g, const double* image, int nx, int ny,
                        const double* viewAngles, int nView, double* sino, int nThreads);
 
+/* ---- if2 --comp: ImageFile::comparativeStatistics -> out = {d, r, e}; 0 if empty ---- */
+int ora_image_compare(const float* a, const float* b, int nx, int ny, double out[3]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,6 +92,7 @@ def lib():
         _LIB.ora_collect_ellipsoids.argtypes = [C.POINTER(_Scanner), p, i, d, d, p, p, i]
         _LIB.ora_ellipse_gradient.argtypes = [C.POINTER(_Scanner), C.POINTER(_Phantom), p, p]
         _LIB.ora_interpolate_to_parallel.argtypes = [C.POINTER(Geom), d, d, p, p, p, p, p]
+        _LIB.ora_image_compare.argtypes = [p, p, i, i, p]
         _LIB.ora_phantom_to_image.argtypes = [C.POINTER(_Phantom), i, i, d, i, p, p, i]
         _LIB.ora_project_image.argtypes = [C.POINTER(Geom), p, i, i, p, i, p, i]
         _LIB.ora_frequency_response.argtypes = [i, d, d, d]
@@ -340,3 +341,16 @@ def project_image(geom, image, angles, nthreads=None):
     lib().ora_project_image(C.byref(geom), _ptr(image), image.shape[0], image.shape[1],
                             _ptr(angles), len(angles), _ptr(sino), nthreads or nthreads_default())
     return sino
+
+
+def image_compare(a, b):
+    """ImageFile::comparativeStatistics of two FP32 images [nx, ny] (column-major
+    storage, v[ix][iy]): (d, r, e)."""
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    assert a.shape == b.shape and a.ndim == 2
+    out = np.zeros(3, np.float64)
+    rc = lib().ora_image_compare(_ptr(a), _ptr(b), a.shape[0], a.shape[1], _ptr(out))
+    if rc == 0:
+        raise ValueError("comparativeStatistics: empty image")
+    return tuple(out)

@@ -15,6 +15,9 @@
 //       private image per thread, images summed: src/threadrecon.cpp:176-255)
 //   ref_harness rebin   IN.pj OUT.pj
 //       Projections::interpolateToParallel (libctsim/projections.cpp:1250-1328)
+//   ref_harness comp    A.if B.if
+//       ImageFile::comparativeStatistics (libctsim/imagefile.cpp:186-240),
+//       printed as "d r e" with 17 significant digits
 //   ref_harness timeraysum PHM NDET NVIEW NRAY GEOM NTHREADS [NVIEWS]
 //       times Scanner::collectProjections over view sub-ranges per thread
 //       (libctsim/scanner.cpp:295-298)
@@ -155,14 +158,25 @@ static int cmdRebin(int argc, char** argv) {
   return ok ? 0 : 2;
 }
 
+static int cmdComp(int argc, char** argv) {
+  if (argc < 4) return 2;
+  ImageFile a, b;
+  if (!a.fileRead(argv[2]) || !b.fileRead(argv[3])) { fprintf(stderr, "if read fail\n"); return 2; }
+  double d = 0, r = 0, e = 0;
+  if (!a.comparativeStatistics(b, d, r, e)) { printf("false\n"); return 0; }
+  printf("%.17g %.17g %.17g\n", d, r, e);
+  return 0;
+}
+
 int main(int argc, char** argv) {
-  if (argc < 2) { fprintf(stderr, "usage: ref_harness filter|bp|timerec|timeraysum|rebin ...\n"); return 2; }
+  if (argc < 2) { fprintf(stderr, "usage: ref_harness filter|bp|timerec|timeraysum|rebin|comp ...\n"); return 2; }
   std::string c = argv[1];
   if (c == "filter") return cmdFilter(argc, argv);
   if (c == "bp") return cmdBackproject(argc, argv);
   if (c == "timerec") return cmdTimeRec(argc, argv);
   if (c == "timeraysum") return cmdTimeRaysum(argc, argv);
   if (c == "rebin") return cmdRebin(argc, argv);
+  if (c == "comp") return cmdComp(argc, argv);
   fprintf(stderr, "unknown command %s\n", argv[1]);
   return 2;
 }

@@ -166,6 +166,60 @@ def make_raster(tmp):
     np.savez_compressed(os.path.join(HERE, "raster.npz"), **out)
 
 
+# device-resident file I/O: reference-written .pj files byte for byte, pj2if
+# images, and comparativeStatistics (if2 --comp) of image pairs
+IO_SCANS = ["herman_eql", "shepp_eqa_even", "pulse_par"]
+
+
+def make_io(tmp):
+    from ctsim_gb300.fileio import ImageFileData, write_if
+    out = {}
+    for name in IO_SCANS:
+        pjf = os.path.join(tmp, name + ".pj")
+        sc = [s for s in SCANS if s[0] == name][0]
+        run(REF, "phm2pj", pjf, sc[3], sc[4], "--phantom", sc[1], "--geometry", sc[2],
+            "--nray", sc[5], *sc[6])
+        with open(pjf, "rb") as f:
+            out[name + "/pj"] = np.frombuffer(f.read(), np.uint8)
+        iff = os.path.join(tmp, name + ".if")
+        run(REF, "pj2if", pjf, iff)
+        im = read_if(iff)
+        out[name + "/pj2if"] = im.data
+        with open(iff, "rb") as f:
+            out[name + "/pj2if_head"] = np.frombuffer(f.read(88), np.uint8)
+        out[name + "/pj2if_labels"] = np.array([[l[0], l[1]] for l in im.labels], dtype=object)
+    # image pairs: rasteriser vs reconstruction, odd sizes, identical, random
+    fa, fb = os.path.join(tmp, "a.if"), os.path.join(tmp, "b.if")
+    pjs = os.path.join(tmp, "s.pj")
+    run(REF, "phm2pj", pjs, 64, 50, "--phantom", "shepp-logan", "--nray", 1)
+    rng = np.random.default_rng(77)
+    pairs = []
+    for k in range(5):
+        if k == 0:
+            run(REF, "phm2if", fa, 64, 64, "--phantom", "shepp-logan", "--nsample", 2)
+            run(REF, "pjrec", pjs, fb, 64, 64, "--filter", "abs_hamming", "--filter-param", 0.54)
+        elif k == 1:
+            run(REF, "phm2if", fa, 33, 47, "--phantom", "herman", "--nsample", 3)
+            run(REF, "phm2if", fb, 33, 47, "--phantom", "herman", "--nsample", 1)
+        elif k == 2:
+            run(REF, "phm2if", fa, 40, 40, "--phantom", "herman", "--nsample", 2)
+            run(REF, "phm2if", fb, 40, 40, "--phantom", "herman", "--nsample", 2)
+        else:
+            nx, ny = ((5, 6), (41, 30))[k - 3]
+            for fn in (fa, fb):
+                d = (rng.standard_normal((nx, ny)) * 3 + 1).astype(np.float32)
+                write_if(fn, ImageFileData(nx, ny, 7, 4, 1, data=d))
+        r = subprocess.run([HARN, "comp", fa, fb], check=True, capture_output=True, text=True)
+        out["comp/%d/a" % k] = read_if(fa).data
+        out["comp/%d/b" % k] = read_if(fb).data
+        out["comp/%d/dre" % k] = np.array([float(x) for x in r.stdout.split()], np.float64)
+        if k == 0:
+            r = subprocess.run([REF, "if2", fa, fb, "--comp"], check=True, capture_output=True,
+                               text=True)
+            out["comp/0/printed"] = np.array(r.stdout)
+    np.savez_compressed(os.path.join(HERE, "io.npz"), **out)
+
+
 def main():
     for b in (REF, REF64, HARN):
         if not os.path.exists(b):
@@ -182,6 +236,8 @@ def main():
             make_rebin(tmp)
         if "raster" in only:
             make_raster(tmp)
+        if not only or "io" in only:
+            make_io(tmp)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print("%-14s %8d bytes" % (f, os.path.getsize(os.path.join(HERE, f))))

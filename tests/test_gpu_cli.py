@@ -92,3 +92,44 @@ def test_phm2if_matches_reference(tool, golden, tmp_path):
                                            % (int(n), int(n), int(ns), phm))
     rc, out = run(tool, "phm2if", tmp_path / "x.if", 8, 8)
     assert rc == 1 and "No phantom defined" in out
+
+
+@pytest.mark.parametrize("name", ["herman_eql", "pulse_par"])
+def test_pj2if_matches_reference(tool, golden, tmp_path, name):
+    from ctsim_gb300.fileio import read_if
+    g = golden("io")
+    pj = tmp_path / "in.pj"
+    pj.write_bytes(g[name + "/pj"].tobytes())
+    out = tmp_path / "out.if"
+    rc, log = run(tool, "pj2if", pj, out, "--polar")
+    assert rc == 0, log
+    raw = out.read_bytes()
+    assert raw[:88] == g[name + "/pj2if_head"].tobytes()
+    im = read_if(out)
+    np.testing.assert_array_equal(im.data, g[name + "/pj2if"])
+    assert [[l[0], l[1]] for l in im.labels] == g[name + "/pj2if_labels"].tolist()
+    rc, log = run(tool, "pj2if", tmp_path / "missing.pj", out)
+    assert rc == 1
+
+
+def test_if2_comp_and_arithmetic(tool, golden, tmp_path):
+    from ctsim_gb300.fileio import ImageFileData, read_if, write_if
+    g = golden("io")
+    fa, fb = tmp_path / "a.if", tmp_path / "b.if"
+    a, b = g["comp/0/a"], g["comp/0/b"]
+    write_if(fa, ImageFileData(64, 64, 7, 4, 1, data=a), [(1, "image a", 0.5, (2020, 1, 1, 0, 0, 0))])
+    write_if(fb, ImageFileData(64, 64, 7, 4, 1, data=b), [(1, "image b", 0.25, (2020, 1, 1, 0, 0, 0))])
+    rc, out = run(tool, "if2", fa, fb, "--comp")
+    assert rc == 0, out
+    assert out == str(g["comp/0/printed"])   # d=..., r=..., e=... as the reference prints it
+    fo = tmp_path / "o.if"
+    rc, out = run(tool, "if2", fa, fb, fo, "--sub")
+    assert rc == 0, out
+    o = read_if(fo)
+    np.testing.assert_array_equal(o.data, a - b)
+    assert [l[1] for l in o.labels] == ["if2 file 1: image a", "if2 file 2: image b",
+                                        "Subtract Images"]
+    fc = tmp_path / "c.if"
+    write_if(fc, ImageFileData(3, 64, 7, 4, 1, data=a[:3]))
+    rc, out = run(tool, "if2", fa, fc, "--comp")
+    assert rc == 1 and "do not match" in out
