@@ -337,6 +337,120 @@ def helical_3d(args, torch, cg, device, phantoms, rank):
                     "value": pv / (fbp_ms / 1e3), "unit": UNIT}}
 
 
+def files_io(args, torch, cg, device, sinos, angles, images, B):
+    """Files on device-resident data, on the main workload's B sinograms and
+    images: the .pj record pack / unpack kernels and pj2if's transpose over all
+    B x 720 views (135 MB each way, larger than L2), if2 --comp's statistics
+    over the B image pairs in one call (kernels, and the host-result call),
+    and .pj files written and read straight from and to device memory
+    (page-cache files)."""
+    import tempfile
+    stream = torch.cuda.current_stream()
+    nv = B * N_VIEW
+    flat = sinos.view(nv, -1)
+    ang = torch.from_numpy(np.tile(np.asarray(angles, np.float64), B)).cuda()
+    rec = torch.empty(nv * (3 + N_DET), dtype=torch.int32, device="cuda")
+    back = torch.empty_like(flat)
+    back_ang = torch.empty_like(ang)
+    status = torch.tensor([0, -1], dtype=torch.int32, device="cuda")
+    L = cg._lib.lib()
+    C = __import__("ctypes")
+    sh = device.stream_handle()
+
+    def pack():
+        cg._lib.check(L.ctgpu_pj_pack(C.c_void_p(flat.data_ptr()), flat.shape[1],
+                                      C.c_void_p(ang.data_ptr()), nv, N_DET,
+                                      C.c_void_p(rec.data_ptr()), sh))
+
+    def unpack():
+        cg._lib.check(L.ctgpu_pj_unpack(C.c_void_p(rec.data_ptr()), nv, N_DET,
+                                        C.c_void_p(back.data_ptr()), back.shape[1],
+                                        C.c_void_p(back_ang.data_ptr()),
+                                        C.c_void_p(status.data_ptr()), sh))
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    reps = max(args.steps, 3)
+    pack_ms = timed(pack, reps)
+    unpack_ms = timed(unpack, reps)
+    ok_records = bool(torch.equal(back[:, :N_DET], flat[:, :N_DET]) and torch.equal(back_ang, ang))
+    rec_bytes = nv * (12 + 4 * N_DET)
+    pack_bytes = nv * (4 * N_DET + 8) + rec_bytes
+    unpack_bytes = rec_bytes + nv * (4 * flat.shape[1] + 8)
+    # pj2if's transpose over all B x 720 views at once (135 MB each way)
+    imgs_t = torch.empty((N_DET, nv), dtype=torch.float32, device="cuda")
+    tr_ms = timed(lambda: device.sino_to_image(flat, N_DET, out=imgs_t), reps)
+    other = images + 1e-3 * torch.randn_like(images)
+    dre = torch.empty((B, 3), dtype=torch.float64, device="cuda")
+    cmp_ms = timed(lambda: device.image_compare_device(images, other, out=dre), reps)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        host_dre = device.image_compare(images, other)
+    cmp_host_ms = (time.perf_counter() - t0) / reps * 1e3
+    ok_cmp = bool(np.array_equal(host_dre, dre.cpu().numpy()))
+    # files: B .pj files written from and read back to device memory
+    tmpd = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    info = cg._lib.PjInfo()
+    info.geometry.n_view, info.geometry.n_det = N_VIEW, N_DET
+    rd = torch.empty_like(sinos)
+    rd_ang = torch.empty((B, N_VIEW), dtype=torch.float64, device="cuda")
+    ang1 = ang[:N_VIEW].contiguous()
+    with tempfile.TemporaryDirectory(dir=tmpd) as td:
+        paths = [os.path.join(td, "s%02d.pj" % b) for b in range(B)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for b in range(B):
+            device.write_pj(paths[b], info, "bench", sinos[b], ang1)
+        w_s = time.perf_counter() - t0
+        fbytes = sum(os.path.getsize(p) for p in paths)
+        t0 = time.perf_counter()
+        for b in range(B):
+            n = C.c_int()
+            cg._lib.check(L.ctgpu_pj_read_device(paths[b].encode(), C.c_void_p(rd[b].data_ptr()),
+                                                 rd.shape[2], C.c_void_p(rd_ang[b].data_ptr()),
+                                                 C.byref(n), sh))
+        r_s = time.perf_counter() - t0
+    ok_files = bool(torch.equal(rd[:, :, :N_DET], sinos[:, :, :N_DET]))
+    hbm, src, _ = peaks()
+
+    def gbs(nbytes, ms):
+        return nbytes / (ms / 1e3) / 1e9
+
+    return {
+        "workload": "%d sinograms 720 x 733 (pitch %d), %d images 512 x 512" % (B, flat.shape[1], B),
+        "pj_pack": {"ms": pack_ms, "views": nv, "algorithmic_bytes": pack_bytes,
+                    "gbs": gbs(pack_bytes, pack_ms), "frac_hbm": gbs(pack_bytes, pack_ms) / hbm},
+        "pj_unpack": {"ms": unpack_ms, "algorithmic_bytes": unpack_bytes,
+                      "gbs": gbs(unpack_bytes, unpack_ms),
+                      "frac_hbm": gbs(unpack_bytes, unpack_ms) / hbm,
+                      "round_trip_exact": ok_records},
+        "pj2if_transpose": {"ms": tr_ms, "views": nv,
+                            "gbs": gbs(8 * nv * N_DET, tr_ms),
+                            "frac_hbm": gbs(8 * nv * N_DET, tr_ms) / hbm},
+        "if2_compare": {"ms": cmp_ms, "pairs": B, "launches": 2,
+                        "algorithmic_bytes": 8 * B * NX * NX,
+                        "gbs": gbs(8 * B * NX * NX, cmp_ms),
+                        "frac_hbm": gbs(8 * B * NX * NX, cmp_ms) / hbm,
+                        "host_call_ms": cmp_host_ms, "host_equals_device": ok_cmp},
+        "pj_files": {"files": B, "bytes": fbytes, "write_gbs": fbytes / w_s / 1e9,
+                     "read_gbs": fbytes / r_s / 1e9, "round_trip_exact": ok_files,
+                     "storage": tmpd or "default temp directory"},
+        "hbm_peak_gbs": hbm, "hbm_peak_source": src,
+    }
+
+
 def run_gpu(args):
     import torch
     import ctsim_gb300 as cg
@@ -437,6 +551,7 @@ def run_gpu(args):
     batched = batched_uneven(args, torch, cg, device, phantoms, rank) \
         if args.batched_problems > 0 else None
     helical = helical_3d(args, torch, cg, device, phantoms, rank) if args.helical else None
+    files = files_io(args, torch, cg, device, sinos, angles[0], images, B) if args.files else None
 
     if rank != 0:
         return 0
@@ -496,6 +611,7 @@ def run_gpu(args):
         "gpu_launches": steps * 4,
         "batched_uneven": batched,
         "helical": helical,
+        "files": files,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))
@@ -515,6 +631,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--helical", type=int, default=1,
                     help="measure the helical 3-D workload after the main one (0: skip)")
+    ap.add_argument("--files", type=int, default=1,
+                    help="measure the device-resident file I/O after the main workload (0: skip)")
     ap.add_argument("--batched-problems", type=int, default=64,
                     help="problems of the uneven batch measured after the main workload (0: skip)")
     ap.add_argument("--ref-views", type=int, default=None,

@@ -131,12 +131,15 @@ SIGNATURES = {
     "ctgpu_pj_read_header": ([_s, C.POINTER(PjInfo), _s, _i], _i),
     "ctgpu_pj_read_device": ([_s, _p, _i, _p, C.POINTER(_i), _p], _i),
     "ctgpu_pj_write_device": ([_s, C.POINTER(PjInfo), _s, _p, _i, _p, _p], _i),
+    "ctgpu_pj_pack": ([_p, _i, _p, _i, _i, _p, _p], _i),
+    "ctgpu_pj_unpack": ([_p, _i, _i, _p, _i, _p, _p, _p], _i),
     "ctgpu_if_read_header": ([_s, C.POINTER(IfInfo)], _i),
     "ctgpu_if_read_labels": ([_s, C.POINTER(IfLabel), _i, _s, C.c_size_t, C.POINTER(_i)], _i),
     "ctgpu_if_read_device": ([_s, _p, _p], _i),
     "ctgpu_if_write_device": ([_s, C.POINTER(IfInfo), C.POINTER(IfLabel), _i, _p, _p], _i),
     "ctgpu_sino_to_image": ([_p, _i, _i, _i, _p, _p], _i),
     "ctgpu_image_compare": ([_p, _p, _i, _i, _i, C.c_size_t, _p, _p], _i),
+    "ctgpu_image_compare_device": ([_p, _p, _i, _i, _i, C.c_size_t, _p, _p], _i),
     "ctgpu_image_arith": ([_s, _p, _p, _p, C.c_size_t, _p], _i),
     "ctgpu_backproject_diff_noalloc": ([C.POINTER(Geometry), _i, _i, _s, C.POINTER(Roi), _p, _i,
                                         _p, _i, _p, _i, _p], _i),

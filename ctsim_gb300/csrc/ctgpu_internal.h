@@ -257,15 +257,15 @@ cudaError_t launch_f64_to_f32(const double* in, float* out, size_t n, cudaStream
 // op 0 add, 1 subtract, 2 multiply, 3 divide (FP32)
 cudaError_t launch_image_arith(int op, const float* a, const float* b, float* out, size_t n,
                                cudaStream_t s);
-// comparative statistics of image pairs: part holds nImages x compare_blocks(nx, ny)
-// x kCmpParts doubles, out nImages x (d, r, e)
-constexpr int kCmpParts = 6;
+// comparative statistics of image pairs (nx * ny < 2^31): part holds nImages x
+// compare_blocks(nx, ny) x kCmpParts float pairs, out nImages x (d, r, e)
+constexpr int kCmpParts = 7;
 struct CompareLaunch {
   const float* a;
   const float* b;
   size_t strideA, strideB;   // floats between images
   int nx, ny, nImages;
-  double* part;
+  float2* part;
   double* out;
 };
 int compare_blocks(int nx, int ny);

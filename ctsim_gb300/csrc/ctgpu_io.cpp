@@ -214,7 +214,8 @@ int ctgpu_pj_read_device(const char* filename, float* d_sino, int pitch, double*
   cudaStream_t st = (cudaStream_t)stream;
   const size_t rec = 12 + 4 * (size_t)nDet;
   const int vpc = (int)std::max<size_t>(1, kChunk / rec);
-  const size_t chunkBytes = rec * (size_t)std::min(vpc, std::max(nView, 1));
+  // slots start on 256-byte boundaries (the record kernels move 16-byte words there)
+  const size_t chunkBytes = (rec * (size_t)std::min(vpc, std::max(nView, 1)) + 255) & ~(size_t)255;
   Stream2 io(st);
   CUDA_TRY(io.init(chunkBytes, 2 * chunkBytes + 16));
   unsigned int* status = reinterpret_cast<unsigned int*>(io.dev + 2 * chunkBytes);
@@ -283,7 +284,8 @@ int ctgpu_pj_write_device(const char* filename, const ctgpu_pj_info* info, const
   cudaStream_t st = (cudaStream_t)stream;
   const size_t rec = 12 + 4 * (size_t)nDet;
   const int vpc = (int)std::max<size_t>(1, kChunk / rec);
-  const size_t chunkBytes = rec * (size_t)std::min(vpc, std::max(nView, 1));
+  // slots start on 256-byte boundaries (the record kernels move 16-byte words there)
+  const size_t chunkBytes = (rec * (size_t)std::min(vpc, std::max(nView, 1)) + 255) & ~(size_t)255;
   Stream2 io(st);
   CUDA_TRY(io.init(chunkBytes, 2 * chunkBytes));
   int pendingViews = 0;   // views of chunk k - 1 in slot (k - 1) & 1
@@ -469,28 +471,51 @@ int ctgpu_if_write_device(const char* filename, const ctgpu_if_info* info,
   return ok();
 }
 
+int ctgpu_pj_pack(const float* d_sino, int pitch, const double* d_angles, int n_view, int n_det,
+                  void* d_records, void* stream) {
+  if (!d_sino || !d_angles || !d_records) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (n_view < 0 || n_det < 0 || pitch < n_det) return fail(CTGPU_ERR_INVALID, "bad sizes");
+  if (reinterpret_cast<uintptr_t>(d_records) & 3)
+    return fail(CTGPU_ERR_INVALID, "d_records must be 4-byte aligned");
+  CUDA_TRY(launch_pj_pack(d_sino, pitch, d_angles, n_view, n_det,
+                          static_cast<uint32_t*>(d_records), (cudaStream_t)stream));
+  return ok();
+}
+
+int ctgpu_pj_unpack(const void* d_records, int n_view, int n_det, float* d_sino, int pitch,
+                    double* d_angles, unsigned int* d_status, void* stream) {
+  if (!d_records || !d_sino || !d_angles || !d_status)
+    return fail(CTGPU_ERR_INVALID, "null argument");
+  if (n_view < 0 || n_det < 0 || pitch < n_det) return fail(CTGPU_ERR_INVALID, "bad sizes");
+  if (reinterpret_cast<uintptr_t>(d_records) & 3)
+    return fail(CTGPU_ERR_INVALID, "d_records must be 4-byte aligned");
+  CUDA_TRY(launch_pj_unpack(static_cast<const uint32_t*>(d_records), n_view, n_det, d_sino, pitch,
+                            d_angles, 0, d_status, (cudaStream_t)stream));
+  return ok();
+}
+
 int ctgpu_sino_to_image(const float* d_sino, int pitch, int n_view, int n_det, float* d_image,
                         void* stream) {
   if (!d_sino || !d_image) return fail(CTGPU_ERR_INVALID, "null argument");
   if (n_view < 0 || n_det < 0 || pitch < n_det) return fail(CTGPU_ERR_INVALID, "bad sizes");
-  if ((n_view + 31) / 32 > 65535) return fail(CTGPU_ERR_INVALID, "too many views");
+  if ((n_view + 63) / 64 > 65535) return fail(CTGPU_ERR_INVALID, "too many views");
   CUDA_TRY(launch_sino_to_image(d_sino, pitch, n_view, n_det, d_image, (cudaStream_t)stream));
   return ok();
 }
 
-int ctgpu_image_compare(const float* d_a, const float* d_b, int n_images, int nx, int ny,
-                        size_t image_stride, double* h_dre, void* stream) {
-  if (!d_a || !d_b || !h_dre) return fail(CTGPU_ERR_INVALID, "null argument");
+int ctgpu_image_compare_device(const float* d_a, const float* d_b, int n_images, int nx, int ny,
+                               size_t image_stride, double* d_dre, void* stream) {
+  if (!d_a || !d_b || !d_dre) return fail(CTGPU_ERR_INVALID, "null argument");
   if (n_images < 1 || n_images > 65535 || nx < 1 || ny < 1)
     return fail(CTGPU_ERR_INVALID, "bad sizes (the reference returns false for an empty image)");
+  if ((size_t)nx * ny >= (1ull << 31)) return fail(CTGPU_ERR_INVALID, "image too large (nx * ny >= 2^31)");
   if (n_images > 1 && image_stride < (size_t)nx * ny)
     return fail(CTGPU_ERR_INVALID, "image_stride < nx * ny");
   cudaStream_t st = (cudaStream_t)stream;
   const int nb = compare_blocks(nx, ny);
-  const size_t partBytes = sizeof(double) * (size_t)n_images * nb * kCmpParts;
-  const size_t outBytes = sizeof(double) * 3 * (size_t)n_images;
-  double* scratch = nullptr;
-  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&scratch), partBytes + outBytes, st));
+  float2* scratch = nullptr;
+  CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&scratch),
+                           sizeof(float2) * (size_t)n_images * nb * kCmpParts, st));
   CompareLaunch L{};
   L.a = d_a;
   L.b = d_b;
@@ -499,11 +524,28 @@ int ctgpu_image_compare(const float* d_a, const float* d_b, int n_images, int nx
   L.ny = ny;
   L.nImages = n_images;
   L.part = scratch;
-  L.out = scratch + partBytes / sizeof(double);
-  cudaError_t e = launch_image_compare(L, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h_dre, L.out, outBytes, cudaMemcpyDeviceToHost, st);
+  L.out = d_dre;
+  const cudaError_t e = launch_image_compare(L, st);
   cudaFreeAsync(scratch, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(CTGPU_ERR_CUDA, std::string("image compare: ") + cudaGetErrorString(e));
+  return ok();
+}
+
+int ctgpu_image_compare(const float* d_a, const float* d_b, int n_images, int nx, int ny,
+                        size_t image_stride, double* h_dre, void* stream) {
+  if (!h_dre) return fail(CTGPU_ERR_INVALID, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  double* out = nullptr;
+  if (n_images >= 1 && n_images <= 65535)
+    CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&out), sizeof(double) * 3 * n_images, st));
+  int rc = ctgpu_image_compare_device(d_a, d_b, n_images, nx, ny, image_stride, out, stream);
+  cudaError_t e = cudaSuccess;
+  if (rc == CTGPU_OK)
+    e = cudaMemcpyAsync(h_dre, out, sizeof(double) * 3 * n_images, cudaMemcpyDeviceToHost, st);
+  if (out) cudaFreeAsync(out, st);
+  const cudaError_t es = cudaStreamSynchronize(st);
+  if (rc != CTGPU_OK) return rc;
+  if (e == cudaSuccess) e = es;
   if (e != cudaSuccess) return fail(CTGPU_ERR_CUDA, std::string("image compare: ") + cudaGetErrorString(e));
   return ok();
 }

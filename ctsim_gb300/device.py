@@ -380,6 +380,36 @@ def write_pj(path, info, remark, sino, angles, stream=None):
                                       stream_handle(stream)))
 
 
+def pj_pack(sino, n_det, angles, out=None, stream=None):
+    """.pj view records of a device sinogram, device to device (ctgpu_pj_pack):
+    an int32 tensor of n_view * (3 + n_det) words (the bytes of the file after
+    its header)."""
+    torch = _torch()
+    nv = sino.shape[0]
+    if out is None:
+        out = torch.empty(nv * (3 + n_det), dtype=torch.int32, device=sino.device)
+    check(lib().ctgpu_pj_pack(_ptr(sino), sino.shape[1], _ptrd(angles), nv, n_det,
+                              C.c_void_p(out.data_ptr()), stream_handle(stream)))
+    return out
+
+
+def pj_unpack(records, n_view, n_det, sino=None, angles=None, stream=None):
+    """Inverse of pj_pack (ctgpu_pj_unpack): returns (sino [n_view, pitch],
+    angles, records whose detector count differs from n_det, first such view)."""
+    torch = _torch()
+    dev = records.device
+    if sino is None:
+        sino = torch.empty((n_view, pitch_for(n_det)), dtype=torch.float32, device=dev)
+    if angles is None:
+        angles = torch.empty((n_view,), dtype=torch.float64, device=dev)
+    status = torch.tensor([0, -1], dtype=torch.int32, device=dev)
+    check(lib().ctgpu_pj_unpack(C.c_void_p(records.data_ptr()), n_view, n_det, _ptr(sino),
+                                sino.shape[1], _ptrd(angles), C.c_void_p(status.data_ptr()),
+                                stream_handle(stream)))
+    st = status.cpu().numpy().view(np.uint32)
+    return sino, angles, int(st[0]), int(st[1])
+
+
 def read_if_header(path):
     info = IfInfo()
     check(lib().ctgpu_if_read_header(enc(str(path)), C.byref(info)))
@@ -453,6 +483,19 @@ def image_compare(a, b, stream=None):
     check(lib().ctgpu_image_compare(_ptr(a), _ptr(b), n, nx, ny, nx * ny,
                                     out.ctypes.data_as(C.c_void_p), stream_handle(stream)))
     return out if batched else tuple(out[0])
+
+
+def image_compare_device(a, b, out=None, stream=None):
+    """image_compare of [n, nx, ny] device images with the results left on the
+    device (out: float64 [n, 3]); no synchronisation."""
+    torch = _torch()
+    assert a.shape == b.shape and a.dim() == 3 and a.is_contiguous() and b.is_contiguous()
+    n, nx, ny = a.shape
+    if out is None:
+        out = torch.empty((n, 3), dtype=torch.float64, device=a.device)
+    check(lib().ctgpu_image_compare_device(_ptr(a), _ptr(b), n, nx, ny, nx * ny, _ptrd(out),
+                                           stream_handle(stream)))
+    return out
 
 
 def image_arith(op, a, b, out=None, stream=None):

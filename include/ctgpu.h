@@ -366,6 +366,18 @@ int ctgpu_pj_read_device(const char* filename, float* d_sino, int pitch, double*
 int ctgpu_pj_write_device(const char* filename, const ctgpu_pj_info* info, const char* remark,
                           const float* d_sino, int pitch, const double* d_angles, void* stream);
 
+/* The view records alone, device to device: what detarrayWrite /
+ * detarrayRead (projections.cpp:811-889) put in a file after the header,
+ * n_view x (12 + 4 n_det) bytes at d_records (4-byte aligned) -- for callers
+ * that move the bytes themselves (their own file layer, a socket, a mapped
+ * file).  Unpack: d_status [2] must start as {0, 0xffffffff}; it receives the
+ * number of records whose detector count differs from n_det and the first
+ * such view; pad columns are zeroed. */
+int ctgpu_pj_pack(const float* d_sino, int pitch, const double* d_angles, int n_view, int n_det,
+                  void* d_records, void* stream);
+int ctgpu_pj_unpack(const void* d_records, int n_view, int n_det, float* d_sino, int pitch,
+                    double* d_angles, unsigned int* d_status, void* stream);
+
 typedef struct {
   int32_t nx, ny;
   int32_t pixel_format;      /* 7 FP32, 8 FP64 (include/array2dfile.h:118-127) */
@@ -416,6 +428,11 @@ int ctgpu_sino_to_image(const float* d_sino, int pitch, int n_view, int n_det, f
  * depend on timing.  An image smaller than 2 x 2 gives e = -1 as there. */
 int ctgpu_image_compare(const float* d_a, const float* d_b, int n_images, int nx, int ny,
                         size_t image_stride, double* h_dre, void* stream);
+/* The same with the results left in device memory (d_dre [n_images][3]):
+ * enqueued on `stream`, no synchronisation (its few KB of scratch are
+ * allocated and freed stream-ordered).  nx * ny must be below 2^31. */
+int ctgpu_image_compare_device(const float* d_a, const float* d_b, int n_images, int nx, int ny,
+                               size_t image_stride, double* d_dre, void* stream);
 /* ImageFile::addImages / subtractImages / multiplyImages / divideImages
  * (imagefile.cpp:378-528) on real FP32 images: op "add" | "subtract" |
  * "multiply" | "divide"; d_out[i] = d_a[i] op d_b[i] for n pixels.  Division

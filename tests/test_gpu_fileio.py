@@ -73,6 +73,31 @@ def test_pj_write_device_is_byte_identical(gpu, golden, tmp_path, name):
     assert out.read_bytes() == path.read_bytes()
 
 
+@pytest.mark.parametrize("name", IO_SCANS)
+def test_pj_pack_unpack_records(gpu, golden, tmp_path, name):
+    """The device-to-device record calls: pack gives the file's bytes after the
+    header; unpack inverts it and flags a record with a wrong detector count."""
+    torch, cg, device, fileio = gpu
+    path = golden_pj(golden, tmp_path, name)
+    ref = fileio.read_pj(path)
+    info, _ = device.read_pj_header(path)
+    sino, ang = to_device(torch, device, ref.data, ref.angles)
+    rec = device.pj_pack(sino, ref.nDet, ang)
+    assert rec.cpu().numpy().tobytes() == path.read_bytes()[info.header_size:]
+    s2, a2, bad, first = device.pj_unpack(rec, ref.nView, ref.nDet)
+    assert bad == 0 and torch.equal(s2, sino) and torch.equal(a2, ang)
+    # records at a 4-byte (not 16-byte) aligned address take the word-by-word path
+    big = torch.zeros(rec.numel() + 1, dtype=torch.int32, device="cuda")
+    device.pj_pack(sino, ref.nDet, ang, out=big[1:])
+    assert torch.equal(big[1:], rec)
+    s3, a3, bad, _ = device.pj_unpack(big[1:], ref.nView, ref.nDet)
+    assert bad == 0 and torch.equal(s3, sino) and torch.equal(a3, ang)
+    rec[(3 + ref.nDet) * 4 + 2] = ref.nDet - 1   # view 4's detector count
+    rec[(3 + ref.nDet) * 6 + 2] = 0              # and view 6's
+    _, _, bad, first = device.pj_unpack(rec, ref.nView, ref.nDet)
+    assert (bad, first) == (2, 4)
+
+
 def test_pj_round_trip_many_chunks(gpu, tmp_path):
     """9216 views x 1024 detectors (38 MB, five 8 MiB chunks each way): the
     device writer's file equals the host restatement's, and reads back exact."""
@@ -195,6 +220,16 @@ def test_image_compare_batched_against_oracle(gpu, oracle):
     a = (rng.standard_normal((8, 512, 512)) * 2 + 0.3).astype(np.float32)
     b = (a + 0.05 * rng.standard_normal(a.shape)).astype(np.float32)
     got = device.image_compare(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda())
+    dev = device.image_compare_device(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda())
+    np.testing.assert_array_equal(dev.cpu().numpy(), got)   # same kernels, same order
+    # an odd-sized batch: unaligned second image, word-by-word loads
+    x = torch.from_numpy(a[:3, :511, :511].copy()).cuda()
+    y = torch.from_numpy(b[:3, :511, :511].copy()).cuda()
+    g3 = device.image_compare(x, y)
+    for i in range(3):
+        want = oracle.image_compare(a[i, :511, :511], b[i, :511, :511])
+        assert g3[i, 2] == want[2]
+        np.testing.assert_allclose(g3[i, :2], want[:2], rtol=REL, atol=0)
     for i in range(8):
         want = oracle.image_compare(a[i], b[i])
         assert got[i, 2] == want[2]
