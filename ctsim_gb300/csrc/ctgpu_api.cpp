@@ -289,7 +289,10 @@ struct ctgpu_recon {
   size_t d_bimage_cap = 0;
   cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
   cudaEvent_t ev[6] = {};   // in_done[2], comp_done[2], out_done[2]
+  double* h_angles_pinned = nullptr;   // page-locked copy of the view angles
+  size_t h_angles_cap = 0;
   ~ctgpu_recon() {
+    if (h_angles_pinned) cudaFreeHost(h_angles_pinned);
     for (void* p : {(void*)d_spec, (void*)d_weights, (void*)d_filtered, (void*)d_angles,
                     (void*)d_views, (void*)d_scratch, (void*)d_sino, (void*)d_image,
                     (void*)d_bsino, (void*)d_bimage})
@@ -1194,42 +1197,63 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
   if (nBatch < 1) return fail(CTGPU_ERR_INVALID, "batch size must be >= 1");
   if (flags & CTGPU_RUN_ACCUMULATE) return fail(CTGPU_ERR_UNSUPPORTED, "batched runs overwrite their images");
   const int nDet = r->g.n_det, nView = r->g.n_view;
-  const int chunk = nBatch < 16 ? nBatch : 16;
-  const size_t sStride = (size_t)nView * r->pitch, iStride = (size_t)r->nx * r->ny;
+  // chunks of 8, 24, then 32 slices: a small first chunk starts the
+  // reconstruction early, larger ones keep the backprojection launches full
+  std::vector<int> sizes, first;
+  for (int left = nBatch, next = 8; left > 0; next = next == 8 ? 24 : 32) {
+    const int n = left < next ? left : next;
+    first.push_back(nBatch - left);
+    sizes.push_back(n);
+    left -= n;
+  }
+  const int chunk = nBatch < 32 ? nBatch : 32;
+  // input rows arrive dense ([slice][view][n_det], one plain copy per chunk);
+  // the filter reads them at pitch n_det and writes the aligned filtered rows
+  const size_t sStride = (size_t)nView * nDet, iStride = (size_t)r->nx * r->ny;
   CUDA_TRY(ensure_device(r->d_bsino, r->d_bsino_cap, 2 * chunk * sStride));
   CUDA_TRY(ensure_device(r->d_bimage, r->d_bimage_cap, 2 * chunk * iStride));
+  if (r->h_angles_cap < (size_t)nView) {
+    if (r->h_angles_pinned) cudaFreeHost(r->h_angles_pinned);
+    r->h_angles_pinned = nullptr;
+    r->h_angles_cap = 0;
+    CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&r->h_angles_pinned),
+                           sizeof(double) * (nView ? nView : 1), cudaHostAllocDefault));
+    r->h_angles_cap = nView;
+  }
   for (cudaStream_t* s : {&r->s_in, &r->s_comp, &r->s_out})
     if (!*s) CUDA_TRY(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking));
   for (cudaEvent_t& e : r->ev)
     if (!e) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  // the per-chunk angle uploads then come from page-locked memory and never
+  // wait for the compute stream on the host (the last call's copies are done:
+  // each call ends synchronised)
+  std::memcpy(r->h_angles_pinned, h_angles, sizeof(double) * nView);
   cudaEvent_t* inDone = r->ev;
   cudaEvent_t* compDone = r->ev + 2;
   cudaEvent_t* outDone = r->ev + 4;
-  const int nChunks = (nBatch + chunk - 1) / chunk;
+  const int nChunks = (int)sizes.size();
   // image copy of chunk c, issued one iteration late so that a pageable
   // destination (whose copy blocks the host) does not hold back the next
   // chunk's input copy and launch
   auto copy_out = [&](int c) -> int {
-    const int b = c & 1, n = nBatch - c * chunk < chunk ? nBatch - c * chunk : chunk;
+    const int b = c & 1;
     CUDA_TRY(cudaStreamWaitEvent(r->s_out, compDone[b], 0));
-    CUDA_TRY(cudaMemcpyAsync(h_images + (size_t)c * chunk * iStride, r->d_bimage + b * chunk * iStride,
-                             sizeof(float) * iStride * n, cudaMemcpyDeviceToHost, r->s_out));
+    CUDA_TRY(cudaMemcpyAsync(h_images + (size_t)first[c] * iStride, r->d_bimage + b * chunk * iStride,
+                             sizeof(float) * iStride * sizes[c], cudaMemcpyDeviceToHost, r->s_out));
     CUDA_TRY(cudaEventRecord(outDone[b], r->s_out));
     return CTGPU_OK;
   };
   for (int c = 0; c < nChunks; c++) {
-    const int b = c & 1, n = nBatch - c * chunk < chunk ? nBatch - c * chunk : chunk;
+    const int b = c & 1, n = sizes[c];
     float* dS = r->d_bsino + b * chunk * sStride;
     float* dI = r->d_bimage + b * chunk * iStride;
     if (c >= 2) CUDA_TRY(cudaStreamWaitEvent(r->s_in, compDone[b], 0));   // buffer b read
-    CUDA_TRY(cudaMemcpy2DAsync(dS, sizeof(float) * r->pitch,
-                               h_sinos + (size_t)c * chunk * nView * nDet, sizeof(float) * nDet,
-                               sizeof(float) * nDet, (size_t)n * nView, cudaMemcpyHostToDevice,
-                               r->s_in));
+    CUDA_TRY(cudaMemcpyAsync(dS, h_sinos + (size_t)first[c] * sStride, sizeof(float) * sStride * n,
+                             cudaMemcpyHostToDevice, r->s_in));
     CUDA_TRY(cudaEventRecord(inDone[b], r->s_in));
     CUDA_TRY(cudaStreamWaitEvent(r->s_comp, inDone[b], 0));
     if (c >= 2) CUDA_TRY(cudaStreamWaitEvent(r->s_comp, outDone[b], 0));   // image b copied out
-    int rc = ctgpu_recon_run_batch(r, n, dS, r->pitch, (long long)sStride, h_angles, dI,
+    int rc = ctgpu_recon_run_batch(r, n, dS, nDet, (long long)sStride, r->h_angles_pinned, dI,
                                    (long long)iStride, flags & CTGPU_RUN_POSTPROCESS, r->s_comp);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(compDone[b], r->s_comp));

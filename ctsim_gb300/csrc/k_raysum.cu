@@ -399,23 +399,28 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
   const float hdelta = g.hdelta, fca0 = g.ca0, fsa0 = g.sa0, Sx = g.Sx, Sy = g.Sy;
   const float CD = (float)L.centerDetectorLength;
 
-  for (int d = threadIdx.x; d < L.nDet; d += blockDim.x) {
+  // ray indices as floats by float arithmetic (exact below 2^24), not by
+  // int-to-float conversions
+  const float fnS = (float)nS, fstep = (float)blockDim.x;
+  float fd = (float)threadIdx.x;
+  for (int d = threadIdx.x; d < L.nDet; d += blockDim.x, fd += fstep) {
     float sum = 0.f;
-    for (int i = 0; i < nS; i++) {
+    float fi = 0.f;
+    for (int i = 0; i < nS; i++, fi += 1.f) {
       const int t = (GEOM == kParallel) ? d : d * nS + i;
-      const float ft = (float)t;
+      const float ft = (GEOM == kParallel) ? fd : fmaf(fd, fnS, fi);
       float rx, ry, invr = 1.f, cj = 1.f, sj = 0.f;
       if (GEOM == kParallel) {
         rx = sdir[i].x;
         ry = sdir[i].y;
       } else if (GEOM == kEquilinear) {
-        rx = fmaf((float)t, stx, rsx);
-        ry = fmaf((float)t, sty, rsy);
+        rx = fmaf(ft, stx, rsx);
+        ry = fmaf(ft, sty, rsy);
         invr = rsqrtf(fmaf(rx, rx, ry * ry));
         rx *= invr;
         ry *= invr;
       } else {
-        float half = (float)t * hdelta;    // phi_t / 2, phi_t = t * delta
+        float half = ft * hdelta;    // phi_t / 2, phi_t = t * delta
         sincosf(half, &sj, &cj);
         float cphi = fmaf(-2.f * sj, sj, 1.f), sphi = 2.f * sj * cj;
         float dxv = CD * (fca0 * cphi - fsa0 * sphi), dyv = CD * (fsa0 * cphi + fca0 * sphi);
@@ -478,7 +483,7 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
         sum = fmaf(ch, e.atten, sum);
       }
     }
-    sino[(size_t)(L.rowOffset + view) * L.pitch + d] = sum / (float)nS;
+    sino[(size_t)(L.rowOffset + view) * L.pitch + d] = sum / fnS;
   }
 }
 

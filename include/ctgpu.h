@@ -214,8 +214,8 @@ int ctgpu_recon_run_batch(ctgpu_recon* r, int n_batch, const float* d_sinos, int
                           void* stream);
 /* ctgpu_recon_run_batch with host buffers: h_sinos n_batch sinograms
  * [n_view][n_det] back to back, h_images n_batch images [nx][ny] back to back.
- * Slices move in chunks of up to 16 through two device buffers, so the copy
- * of one chunk overlaps the reconstruction of the previous one (page-locked
+ * Slices move in chunks of 8, 24, then 32 through two device buffers, so the
+ * copy of one chunk overlaps the reconstruction of the previous one (page-locked
  * host buffers make the copies asynchronous; pageable ones work, with less
  * overlap).  Synchronous: returns when h_images is written.  No reference
  * counterpart (CTSim reconstructs one slice per Reconstructor). */
