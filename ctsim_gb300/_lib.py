@@ -128,6 +128,11 @@ SIGNATURES = {
     "ctgpu_batch_run": ([_p, _p], _i),
     "ctgpu_batch_shape": ([_p, C.POINTER(_i), C.POINTER(_i)], _i),
     "ctgpu_batch_destroy": ([_p], None),
+    "ctgpu_convert_polar": ([C.POINTER(Geometry), _p, _i, _p, _i, _i, _s, _p, _p], _i),
+    "ctgpu_convert_fft_polar": ([C.POINTER(Geometry), _p, _i, _p, _i, _i, _s, _i, _p, _p,
+                                 C.POINTER(_i), _p], _i),
+    "ctgpu_image_ifft_magnitude": ([_p, _p, _i, _i, _p, _p], _i),
+    "ctgpu_reconstruct_fourier": ([C.POINTER(Geometry), _p, _i, _p, _i, _i, _s, _i, _p, _p], _i),
     "ctgpu_pj_read_header": ([_s, C.POINTER(PjInfo), _s, _i], _i),
     "ctgpu_pj_read_device": ([_s, _p, _i, _p, C.POINTER(_i), _p], _i),
     "ctgpu_pj_write_device": ([_s, C.POINTER(PjInfo), _s, _p, _i, _p, _p], _i),

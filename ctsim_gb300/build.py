@@ -29,14 +29,14 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17",
                   "-I" + os.path.join(ROOT, "include")]
 # per-file device flags: the helical weights are FP64 expressions the
 # reference evaluates without fused multiply-adds
-FILE_FLAGS = {"k_helical.cu": ["--fmad=false"]}
+FILE_FLAGS = {"k_helical.cu": ["--fmad=false"], "k_fourier.cu": ["--fmad=false"]}
 # extra nvcc flags for every translation unit, e.g. tuning macros
 # (CTGPU_NVCC_FLAGS="-DCTGPU_BP_CTAS_PER_SM=5")
 EXTRA_FLAGS = os.environ.get("CTGPU_NVCC_FLAGS", "").split()
 
 LIB_SOURCES = ["k_common.cu", "k_raysum.cu", "k_filter.cu", "k_backproject.cu", "k_helical.cu",
                "ctgpu_api.cpp", "filter_design.cpp", "ctsim_api.cpp", "k_noalloc.cu", "k_rebin.cu",
-               "k_fileio.cu", "ctgpu_io.cpp"]
+               "k_fileio.cu", "ctgpu_io.cpp", "k_fourier.cu", "ctgpu_fourier.cpp"]
 TOOL_SOURCES = ["tools/ctsimtext.cpp"]
 
 
@@ -49,7 +49,7 @@ def nvcc():
 
 def _headers():
     hs = [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
-    hs += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    hs += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     return hs
 
 

@@ -271,4 +271,41 @@ struct CompareLaunch {
 int compare_blocks(int nx, int ny);
 cudaError_t launch_image_compare(const CompareLaunch& L, cudaStream_t s);
 
+// ----- polar and direct-Fourier images (k_fourier.cu) ----------------------
+struct PolarLaunch {
+  int nx, ny, cols;            // columns >= cols are zeroed
+  const double* xs;            // [nx] pixel-centre x, accumulated as the reference does
+  const double* ys;            // [ny]
+  double rotInc, rotStart, detInc, detCenter;
+  const float* data;           // [nView][pitch] real rows, or float2 [nView][pitch]
+  int complexData, pitch, nView, nPos;
+  int interp;                  // 0 nearest, 1 bilinear
+  float* outRe;
+  float* outIm;                // may be null
+};
+cudaError_t launch_polar(const PolarLaunch& L, cudaStream_t s);
+
+struct FourierViewsLaunch {
+  const float* sino;           // parallel rows [nView][pitch]
+  int pitch, nView, nDet;
+  int nInterp, N, iMid;        // points interpolated, transform length, insertion point
+  const double* posTable;      // [nInterp] detector positions of the interpolated points
+  double projScale, fftScale;
+  const float2* twiddle;       // [N] exp(-2 pi i m / N)
+  float2* spec;                // [nView][N] out, natural order
+};
+cudaError_t launch_fourier_views(const FourierViewsLaunch& L, cudaStream_t s);
+
+struct IfftLaunch {
+  int nx, ny;
+  const float* inRe;           // [nx][ny]
+  const float* inIm;
+  float2* tmp;                 // [nx][ny] scratch
+  const float2* twX;           // [nx] exp(-2 pi i m / nx)
+  const float2* twY;           // [ny]
+  float* out;                  // [nx][ny] magnitude, natural order
+};
+cudaError_t launch_ifft_magnitude(const IfftLaunch& L, cudaStream_t s);
+size_t line_smem_bytes(int n);
+
 }  // namespace ctgpu

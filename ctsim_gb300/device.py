@@ -507,3 +507,56 @@ def image_arith(op, a, b, out=None, stream=None):
     check(lib().ctgpu_image_arith(enc(op), _ptr(a), _ptr(b), _ptr(out), a.numel(),
                                   stream_handle(stream)))
     return out
+
+
+# ------------------------------------------------- polar / direct Fourier --
+def _angles_ptr(angles):
+    if angles is None:
+        return None, None
+    a = np.ascontiguousarray(angles, np.float64)
+    return a, a.ctypes.data_as(C.c_void_p)
+
+
+def convert_polar(geometry, sino, angles, nx, ny, interp="bilinear", stream=None):
+    """Projections::convertPolar of device rows sino [n_view, pitch]: FP32 [nx, ny]."""
+    torch = _torch()
+    out = torch.empty((nx, ny), dtype=torch.float32, device=sino.device)
+    keep, ap = _angles_ptr(angles)
+    check(lib().ctgpu_convert_polar(C.byref(geometry), _ptr(sino), sino.shape[1], ap, nx, ny,
+                                    enc(interp), _ptr(out), stream_handle(stream)))
+    return out
+
+
+def convert_fft_polar(geometry, sino, angles, nx, ny, interp="bilinear", zeropad=1,
+                      stream=None):
+    """Projections::convertFFTPolar: (real [nx, ny], imag [nx, ny], transform length)."""
+    torch = _torch()
+    re = torch.empty((nx, ny), dtype=torch.float32, device=sino.device)
+    im = torch.empty_like(re)
+    n = C.c_int()
+    keep, ap = _angles_ptr(angles)
+    check(lib().ctgpu_convert_fft_polar(C.byref(geometry), _ptr(sino), sino.shape[1], ap, nx, ny,
+                                        enc(interp), zeropad, _ptr(re), _ptr(im), C.byref(n),
+                                        stream_handle(stream)))
+    return re, im, n.value
+
+
+def image_ifft_magnitude(re, im, stream=None):
+    """ImageFile::ifft + magnitude + shuffleFourierToNaturalOrder."""
+    torch = _torch()
+    out = torch.empty_like(re)
+    check(lib().ctgpu_image_ifft_magnitude(_ptr(re), _ptr(im), re.shape[0], re.shape[1],
+                                           _ptr(out), stream_handle(stream)))
+    return out
+
+
+def reconstruct_fourier(geometry, sino, angles, nx, ny, interp="bilinear", zeropad=1,
+                        stream=None):
+    """The GUI's Fourier reconstruction: convertFFTPolar, ifft, magnitude, shuffle."""
+    torch = _torch()
+    out = torch.empty((nx, ny), dtype=torch.float32, device=sino.device)
+    keep, ap = _angles_ptr(angles)
+    check(lib().ctgpu_reconstruct_fourier(C.byref(geometry), _ptr(sino), sino.shape[1], ap, nx,
+                                          ny, enc(interp), zeropad, _ptr(out),
+                                          stream_handle(stream)))
+    return out

@@ -334,6 +334,39 @@ int ctgpu_helical_plan_run(ctgpu_helical_plan* p, const float* d_in, int in_pitc
 void ctgpu_helical_plan_destroy(ctgpu_helical_plan* p);
 
 /* ------------------------------------------------------------------------ */
+/* Polar and direct-Fourier images -- Projections::convertPolar /            */
+/* convertFFTPolar (libctsim/projections.cpp:953-1180) and the GUI's Fourier */
+/* reconstruction (src/views.cpp:2828-2849).  Fan-beam data is rebinned to   */
+/* parallel rays first (interpolateToParallel), as there; h_view_angles is   */
+/* needed for that only.  interp_name: "nearest" | "bilinear" (the           */
+/* reference's table; its "bicubic" is commented out).  The reference's      */
+/* interpolatePolar loops ix over ny (projections.cpp:1151): columns ix >= ny */
+/* are not computed there and are zero here.  Synchronous.                   */
+/* ------------------------------------------------------------------------ */
+/* convertPolar: d_image [nx][ny] FP32 */
+int ctgpu_convert_polar(const ctgpu_geometry* g, const float* d_sino, int pitch,
+                        const double* h_view_angles, int nx, int ny, const char* interp_name,
+                        float* d_image, void* stream);
+/* convertFFTPolar: the complex image as d_real, d_imag [nx][ny] FP32;
+ * *n_transform (may be NULL) = the zero-padded transform length
+ * (addZeropadFactor of floor(sqrt(nx^2 + ny^2))); FP32 transforms where the
+ * reference uses FFTW in FP64 (which this library does not need). */
+int ctgpu_convert_fft_polar(const ctgpu_geometry* g, const float* d_sino, int pitch,
+                            const double* h_view_angles, int nx, int ny, const char* interp_name,
+                            int zeropad, float* d_real, float* d_imag, int* n_transform,
+                            void* stream);
+/* ImageFile::ifft (backward 2-D DFT after shuffleNaturalToFourierOrder),
+ * ImageFile::magnitude and Fourier::shuffleFourierToNaturalOrder of the
+ * complex image (d_real, d_imag) into d_out [nx][ny] FP32. */
+int ctgpu_image_ifft_magnitude(const float* d_real, const float* d_imag, int nx, int ny,
+                               float* d_out, void* stream);
+/* the GUI's "Reconstruct Fourier": convertFFTPolar, then ctgpu_image_ifft_magnitude */
+int ctgpu_reconstruct_fourier(const ctgpu_geometry* g, const float* d_sino, int pitch,
+                              const double* h_view_angles, int nx, int ny,
+                              const char* interp_name, int zeropad, float* d_image,
+                              void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Files on device-resident data -- .pj / .if I/O (libctsim/projections.cpp: */
 /* 485-889, libctsim/array2dfile.cpp:399-640) and the pj2if / if2 utilities  */
 /* (tools/pj2if.cpp, tools/if2.cpp, libctsim/imagefile.cpp:186-528).  The    */

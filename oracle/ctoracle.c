@@ -1708,3 +1708,294 @@ int ora_image_compare(const float* a, const float* b, int nx, int ny, double out
   out[2] = eMax;
   return 1;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Polar and direct-Fourier images: Projections::convertPolar /             */
+/* convertFFTPolar (projections.cpp:953-1180) and the Fourier               */
+/* reconstruction of the GUI (src/views.cpp:2828-2849): convertFFTPolar,    */
+/* ImageFile::ifft (imagefile.cpp:770-826), magnitude (:1175-1198) and      */
+/* Fourier::shuffleFourierToNaturalOrder (fourier.cpp:31-63).  FFTW's       */
+/* transforms are restated as DFTs (radix-2 for powers of two).             */
+/* ------------------------------------------------------------------------- */
+
+/* Fourier::shuffleFourierToNaturalOrder: new[d] = old[nat_src(n, d)] */
+static int nat_src(int n, int d) {
+  if (n % 2) {
+    const int h = (n - 1) / 2;
+    return d == h ? 0 : (d > h ? d - h : d + h + 1);
+  }
+  const int h = n / 2;
+  return d == h ? 0 : (d < h ? d + h : d - h);
+}
+/* Fourier::shuffleNaturalToFourierOrder: new[d] = old[fou_src(n, d)] */
+static int fou_src(int n, int d) {
+  if (n % 2) {
+    const int h = (n - 1) / 2;
+    return d == 0 ? h : (d <= h ? d + h : d - h - 1);
+  }
+  const int h = n / 2;
+  return d == 0 ? h : (d < h ? d + h : d - h);
+}
+
+/* DFT of n complex values (re, im) in place; sign -1 forward (FFTW_FORWARD),
+   +1 backward; unnormalised */
+static void dft_inplace(double* re, double* im, int n, int sign) {
+  if (n <= 1) return;
+  if ((n & (n - 1)) == 0) {   /* iterative radix-2 Cooley-Tukey */
+    for (int i = 1, j = 0; i < n; i++) {
+      int bit = n >> 1;
+      for (; j & bit; bit >>= 1) j ^= bit;
+      j ^= bit;
+      if (i < j) {
+        double t = re[i]; re[i] = re[j]; re[j] = t;
+        t = im[i]; im[i] = im[j]; im[j] = t;
+      }
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+      for (int k = 0; k < len / 2; k++) {
+        const double a = sign * O_TWOPI * k / len, wr = cos(a), wi = sin(a);
+        for (int i = 0; i < n; i += len) {
+          const int u = i + k, v = i + k + len / 2;
+          const double xr = re[v] * wr - im[v] * wi, xi = re[v] * wi + im[v] * wr;
+          re[v] = re[u] - xr; im[v] = im[u] - xi;
+          re[u] += xr; im[u] += xi;
+        }
+      }
+    }
+    return;
+  }
+  double* tr = malloc(sizeof(double) * n);
+  double* ti = malloc(sizeof(double) * n);
+  for (int k = 0; k < n; k++) {
+    double sr = 0, si = 0;
+    for (int j = 0; j < n; j++) {
+      const double a = sign * O_TWOPI * (double)(((long long)j * k) % n) / n;
+      const double c = cos(a), s = sin(a);
+      sr += re[j] * c - im[j] * s;
+      si += re[j] * s + im[j] * c;
+    }
+    tr[k] = sr; ti[k] = si;
+  }
+  memcpy(re, tr, sizeof(double) * n);
+  memcpy(im, ti, sizeof(double) * n);
+  free(tr); free(ti);
+}
+
+/* Projections::calcArrayPolarCoordinates (projections.cpp:1113-1149) */
+static void polar_coords(int nx, int ny, double viewDiameter, double rotInc, double rotStart,
+                         int nDetWithZeros, double zeropadRatio, double detInc, double* pView,
+                         double* pDet) {
+  double xMin = -viewDiameter / 2, xMax = xMin + viewDiameter;
+  double yMin = -viewDiameter / 2, yMax = yMin + viewDiameter;
+  const double xCent = (xMin + xMax) / 2, yCent = (yMin + yMax) / 2;
+  xMin = (xMin - xCent) * zeropadRatio + xCent;
+  xMax = (xMax - xCent) * zeropadRatio + xCent;
+  yMin = (yMin - yCent) * zeropadRatio + yCent;
+  yMax = (yMax - yCent) * zeropadRatio + yCent;
+  const double xInc = (xMax - xMin) / nx, yInc = (yMax - yMin) / ny;
+  const double detCenter = (nDetWithZeros - 1) / 2.;
+  double x = xMin + xInc / 2;
+  for (int ix = 0; ix < nx; x += xInc, ix++) {
+    double y = yMin + yInc / 2;
+    for (int iy = 0; iy < ny; y += yInc, iy++) {
+      double r = sqrt(x * x + y * y);
+      double phi = atan2(y, x);
+      if (phi <= -rotInc / 2) phi += O_TWOPI;
+      if (phi >= O_PI - (rotInc / 2)) {
+        phi -= O_PI;
+        r = -r;
+      }
+      pView[(size_t)ix * ny + iy] = (phi - rotStart) / rotInc;
+      pDet[(size_t)ix * ny + iy] = (r / detInc) + detCenter;
+    }
+  }
+}
+
+/* BilinearPolarInterpolator::interpolate (include/interpolator.h:110-154) of
+   one component of m [nAngle][nPos] */
+static double bilinear_polar(const double* m, int nAngle, int nPos, double dAngle, double dPos) {
+#define M(a, p) m[(size_t)(a) * nPos + (p)]
+  const int fa0 = (int)floor(dAngle), fp0 = (int)floor(dPos);
+  const double fa = dAngle - fa0, fp = dPos - fp0;
+  if (fa0 < -1 || fp0 < 0 || fa0 > nAngle - 1 || fp0 > nPos - 1) return 0;
+  if (fa0 == -1 && fp0 == nPos - 1) return M(0, nPos - 1) + fa * (M(nAngle - 1, fp0) - M(0, fp0));
+  if (fa0 == nAngle - 1 && fp0 == nPos - 1)
+    return M(nAngle - 1, nPos - 1) + fa * (M(0, fp0) - M(nAngle - 1, fp0));
+  if (fp0 == nPos - 1) return M(fa0, fp0) + fa * (M(fa0 + 1, fp0) - M(fa0, fp0));
+  if (fa0 == nAngle - 1) {
+    const int lo = (nPos - 1) - fp0, up = (nPos - 1) - (fp0 + 1);
+    return (1 - fa) * (1 - fp) * M(fa0, fp0) + fa * (1 - fp) * M(0, lo) +
+           fp * (1 - fa) * M(fa0, fp0 + 1) + fa * fp * M(0, up);
+  }
+  if (fa0 == -1) {
+    const int lo = (nPos - 1) - fp0, up = (nPos - 1) - (fp0 + 1);
+    return (1 - fa) * (1 - fp) * M(nAngle - 1, lo) + fa * (1 - fp) * M(fa0 + 1, fp0) +
+           fp * (1 - fa) * M(nAngle - 1, up) + fa * fp * M(fa0 + 1, fp0 + 1);
+  }
+  return (1 - fa) * (1 - fp) * M(fa0, fp0) + fa * (1 - fp) * M(fa0 + 1, fp0) +
+         fp * (1 - fa) * M(fa0, fp0 + 1) + fa * fp * M(fa0 + 1, fp0 + 1);
+#undef M
+}
+
+/* Projections::interpolatePolar (projections.cpp:1136-1180); its loops run ix
+   over ny as well (:1151), so only columns ix < min(nx, ny) are written */
+static void polar_interp(const double* re, const double* im, int nView, int nPos,
+                         const double* pView, const double* pDet, int nx, int ny, int interp,
+                         float* outRe, float* outIm) {
+  const int cols = nx < ny ? nx : ny;
+  for (int ix = 0; ix < cols; ix++)
+    for (int iy = 0; iy < ny; iy++) {
+      const size_t i = (size_t)ix * ny + iy;
+      double vr = 0, vi = 0;
+      if (interp == 0) {
+        const double a = pView[i], p = pDet[i];
+        unsigned int iv = (unsigned int)(a > 0 ? (int)(a + 0.5) : (int)(a - 0.5));
+        const unsigned int id = (unsigned int)(p > 0 ? (int)(p + 0.5) : (int)(p - 0.5));
+        if (iv == (unsigned int)nView) iv = 0;
+        if (id < (unsigned int)nPos && iv < (unsigned int)nView) {
+          vr = re[(size_t)iv * nPos + id];
+          vi = im ? im[(size_t)iv * nPos + id] : 0;
+        }
+      } else {
+        vr = bilinear_polar(re, nView, nPos, pView[i], pDet[i]);
+        vi = im ? bilinear_polar(im, nView, nPos, pView[i], pDet[i]) : 0;
+      }
+      outRe[i] = (float)vr;
+      if (outIm) outIm[i] = (float)vi;
+    }
+}
+
+/* the parallel projections the polar conversions start from: the input, or
+   interpolateToParallel of fan-beam data (rotStart 0 afterwards) */
+static float* polar_source(const ora_geom* g, double rotStart, double detStart, const float* sino,
+                           const double* angles, double* rs, double* ri, double* di) {
+  float* p = malloc(sizeof(float) * (size_t)g->nView * g->nDet);
+  if (g->geometry == ORA_GEOM_PARALLEL) {
+    memcpy(p, sino, sizeof(float) * (size_t)g->nView * g->nDet);
+    *rs = rotStart; *ri = g->rotInc; *di = g->detInc;
+  } else {
+    double* oa = malloc(sizeof(double) * g->nView);
+    double hdr[3];
+    ora_interpolate_to_parallel(g, rotStart, detStart, sino, angles, p, oa, hdr);
+    free(oa);
+    *rs = 0; *ri = hdr[0]; *di = hdr[2];
+  }
+  return p;
+}
+
+int ora_convert_polar(const ora_geom* g, double rotStart, double detStart, const float* sino,
+                      const double* angles, int nx, int ny, int interp, float* out) {
+  double rs, ri, di;
+  float* p = polar_source(g, rotStart, detStart, sino, angles, &rs, &ri, &di);
+  const size_t n = (size_t)g->nView * g->nDet;
+  double* re = malloc(sizeof(double) * n);
+  for (size_t i = 0; i < n; i++) re[i] = p[i];
+  double* pv = malloc(sizeof(double) * (size_t)nx * ny);
+  double* pd = malloc(sizeof(double) * (size_t)nx * ny);
+  polar_coords(nx, ny, g->viewDiameter, ri, rs, g->nDet, 1., di, pv, pd);
+  memset(out, 0, sizeof(float) * (size_t)nx * ny);
+  polar_interp(re, NULL, g->nView, g->nDet, pv, pd, nx, ny, interp, out, NULL);
+  free(p); free(re); free(pv); free(pd);
+  return 0;
+}
+
+/* ProcessSignal::addZeropadFactor (procsignal.cpp:867-881) */
+int ora_add_zeropad_factor(int n, int zeropad) {
+  if (zeropad > 0) {
+    const double lb = log(n) / log(2);
+    return 1 << ((int)floor(lb) + zeropad);
+  }
+  return n;
+}
+
+int ora_convert_fft_polar(const ora_geom* g, double rotStart, double detStart, const float* sino,
+                          const double* angles, int nx, int ny, int interp, int zeropad,
+                          float* outRe, float* outIm) {
+  double rs, ri, di;
+  float* p = polar_source(g, rotStart, detStart, sino, angles, &rs, &ri, &di);
+  const int nDet = g->nDet, nView = g->nView;
+  const int nInterp = (int)(double)sqrt((double)(unsigned int)(nx * nx + ny * ny));
+  const int N = ora_add_zeropad_factor(nInterp, zeropad);
+  const double projScale = nInterp / (g->viewDiameter * 0.05);
+  const double zpRatio = (double)N / (double)nInterp;
+  const double interpScale = nDet / (double)nInterp;
+  const double fftScale = 1. / (double)(nInterp * nInterp);
+  const int iMid = nInterp / 2;
+  const double dMid = nInterp / 2.;
+  const int zeros = N - nInterp;
+  double* re = malloc(sizeof(double) * (size_t)nView * N);
+  double* im = malloc(sizeof(double) * (size_t)nView * N);
+  double* vr = malloc(sizeof(double) * (N > nInterp ? N : nInterp));
+  double* vi = malloc(sizeof(double) * (N > nInterp ? N : nInterp));
+  double* tr = malloc(sizeof(double) * (N > nInterp ? N : nInterp));
+  for (int v = 0; v < nView; v++) {
+    const float* y = p + (size_t)v * nDet;
+    for (int i = 0; i < nInterp; i++) {   /* LinearInterpolator<float>, zero outside */
+      const double x = (nDet / 2.) + (i - dMid) * interpScale;
+      double r;
+      if (x == 0) r = y[0];
+      else if (x < 0) r = 0;
+      else if (x == nDet - 1) r = y[nDet - 1];
+      else if (x > nDet - 1) r = 0;
+      else {
+        const int f = (int)floor(x);
+        r = y[f] + (y[f + 1] - y[f]) * (x - f);
+      }
+      vr[i] = r * projScale;
+      vi[i] = 0;
+    }
+    for (int d = 0; d < nInterp; d++) tr[d] = vr[nat_src(nInterp, d)];
+    memcpy(vr, tr, sizeof(double) * nInterp);
+    if (zeros > 0) {
+      for (int i = nInterp - 1; i >= iMid; i--) { vr[i + zeros] = vr[i]; vi[i + zeros] = vi[i]; }
+      for (int i = iMid; i < iMid + zeros; i++) vr[i] = vi[i] = 0;
+    }
+    dft_inplace(vr, vi, N, -1);
+    for (int d = 0; d < N; d++) {
+      re[(size_t)v * N + d] = vr[nat_src(N, d)] * fftScale;
+      im[(size_t)v * N + d] = vi[nat_src(N, d)] * fftScale;
+    }
+  }
+  double* pv = malloc(sizeof(double) * (size_t)nx * ny);
+  double* pd = malloc(sizeof(double) * (size_t)nx * ny);
+  polar_coords(nx, ny, g->viewDiameter, ri, rs, N, zpRatio, di * interpScale, pv, pd);
+  memset(outRe, 0, sizeof(float) * (size_t)nx * ny);
+  memset(outIm, 0, sizeof(float) * (size_t)nx * ny);
+  polar_interp(re, im, nView, N, pv, pd, nx, ny, interp, outRe, outIm);
+  free(p); free(re); free(im); free(vr); free(vi); free(tr); free(pv); free(pd);
+  return N;
+}
+
+/* ImageFile::ifft + magnitude + Fourier::shuffleFourierToNaturalOrder of a
+   complex FP32 image [nx][ny] -> out (FP32) */
+void ora_ifft_magnitude(const float* inRe, const float* inIm, int nx, int ny, float* out) {
+  const size_t n = (size_t)nx * ny;
+  double* re = malloc(sizeof(double) * n);
+  double* im = malloc(sizeof(double) * n);
+  /* shuffleNaturalToFourierOrder (fourier.cpp:66-98): each column, then each row */
+  for (int ix = 0; ix < nx; ix++)
+    for (int iy = 0; iy < ny; iy++) {
+      const size_t s = (size_t)fou_src(nx, ix) * ny + fou_src(ny, iy);
+      re[(size_t)ix * ny + iy] = inRe[s];
+      im[(size_t)ix * ny + iy] = inIm[s];
+    }
+  /* FFTW_BACKWARD 2-D DFT, unnormalised: along iy, then along ix */
+  double* cr = malloc(sizeof(double) * (nx > ny ? nx : ny));
+  double* ci = malloc(sizeof(double) * (nx > ny ? nx : ny));
+  for (int ix = 0; ix < nx; ix++) dft_inplace(re + (size_t)ix * ny, im + (size_t)ix * ny, ny, 1);
+  for (int iy = 0; iy < ny; iy++) {
+    for (int ix = 0; ix < nx; ix++) { cr[ix] = re[(size_t)ix * ny + iy]; ci[ix] = im[(size_t)ix * ny + iy]; }
+    dft_inplace(cr, ci, nx, 1);
+    for (int ix = 0; ix < nx; ix++) { re[(size_t)ix * ny + iy] = cr[ix]; im[(size_t)ix * ny + iy] = ci[ix]; }
+  }
+  /* FP32 image, magnitude in FP32 (imagefile.cpp:1189), natural order */
+  float* mag = malloc(sizeof(float) * n);
+  for (size_t i = 0; i < n; i++) {
+    const float r = (float)re[i], m = (float)im[i];
+    mag[i] = sqrtf(r * r + m * m);
+  }
+  for (int ix = 0; ix < nx; ix++)
+    for (int iy = 0; iy < ny; iy++)
+      out[(size_t)ix * ny + iy] = mag[(size_t)nat_src(nx, ix) * ny + nat_src(ny, iy)];
+  free(re); free(im); free(cr); free(ci); free(mag);
+}

@@ -143,6 +143,20 @@ void ora_phantom_to_image(const ora_phantom* p, int nx, int ny, double viewRatio
 int  ora_project_image(const ora_geom* g, const double* image, int nx, int ny,
                        const double* viewAngles, int nView, double* sino, int nThreads);
 
+/* ---- polar / direct-Fourier images (Projections::convertPolar /
+   convertFFTPolar, the GUI's Fourier reconstruction) ---- */
+/* interp: 0 nearest, 1 bilinear; out [nx][ny]; fan-beam input is rebinned
+   first (interpolateToParallel) */
+int  ora_convert_polar(const ora_geom* g, double rotStart, double detStart, const float* sino,
+                       const double* angles, int nx, int ny, int interp, float* out);
+int  ora_add_zeropad_factor(int n, int zeropad);
+/* returns the zero-padded transform length */
+int  ora_convert_fft_polar(const ora_geom* g, double rotStart, double detStart,
+                           const float* sino, const double* angles, int nx, int ny, int interp,
+                           int zeropad, float* outRe, float* outIm);
+/* ImageFile::ifft, magnitude, Fourier::shuffleFourierToNaturalOrder */
+void ora_ifft_magnitude(const float* inRe, const float* inIm, int nx, int ny, float* out);
+
 /* ---- if2 --comp: ImageFile::comparativeStatistics -> out = {d, r, e}; 0 if empty ---- */
 int ora_image_compare(const float* a, const float* b, int nx, int ny, double out[3]);
 

@@ -93,6 +93,11 @@ def lib():
         _LIB.ora_ellipse_gradient.argtypes = [C.POINTER(_Scanner), C.POINTER(_Phantom), p, p]
         _LIB.ora_interpolate_to_parallel.argtypes = [C.POINTER(Geom), d, d, p, p, p, p, p]
         _LIB.ora_image_compare.argtypes = [p, p, i, i, p]
+        _LIB.ora_convert_polar.argtypes = [C.POINTER(Geom), d, d, p, p, i, i, i, p]
+        _LIB.ora_convert_fft_polar.argtypes = [C.POINTER(Geom), d, d, p, p, i, i, i, i, p, p]
+        _LIB.ora_add_zeropad_factor.argtypes = [i, i]
+        _LIB.ora_ifft_magnitude.argtypes = [p, p, i, i, p]
+        _LIB.ora_ifft_magnitude.restype = None
         _LIB.ora_phantom_to_image.argtypes = [C.POINTER(_Phantom), i, i, d, i, p, p, i]
         _LIB.ora_project_image.argtypes = [C.POINTER(Geom), p, i, i, p, i, p, i]
         _LIB.ora_frequency_response.argtypes = [i, d, d, d]
@@ -354,3 +359,42 @@ def image_compare(a, b):
     if rc == 0:
         raise ValueError("comparativeStatistics: empty image")
     return tuple(out)
+
+
+POLAR_INTERP = {"nearest": 0, "bilinear": 1}
+
+
+def convert_polar(geom, rot_start, det_start, sino, angles, nx, ny, interp):
+    """Projections::convertPolar: FP32 image [nx, ny] (columns >= ny stay zero)."""
+    sino = np.ascontiguousarray(sino, np.float32)
+    angles = np.ascontiguousarray(angles, np.float64)
+    out = np.zeros((nx, ny), np.float32)
+    lib().ora_convert_polar(C.byref(geom), rot_start, det_start, _ptr(sino), _ptr(angles), nx, ny,
+                            POLAR_INTERP[interp], _ptr(out))
+    return out
+
+
+def convert_fft_polar(geom, rot_start, det_start, sino, angles, nx, ny, interp, zeropad):
+    """Projections::convertFFTPolar: (real [nx, ny], imag [nx, ny], transform length)."""
+    sino = np.ascontiguousarray(sino, np.float32)
+    angles = np.ascontiguousarray(angles, np.float64)
+    re = np.zeros((nx, ny), np.float32)
+    im = np.zeros((nx, ny), np.float32)
+    n = lib().ora_convert_fft_polar(C.byref(geom), rot_start, det_start, _ptr(sino), _ptr(angles),
+                                    nx, ny, POLAR_INTERP[interp], zeropad, _ptr(re), _ptr(im))
+    return re, im, n
+
+
+def ifft_magnitude(re, im):
+    """ImageFile::ifft, magnitude, shuffleFourierToNaturalOrder of a complex image."""
+    re = np.ascontiguousarray(re, np.float32)
+    im = np.ascontiguousarray(im, np.float32)
+    out = np.zeros_like(re)
+    lib().ora_ifft_magnitude(_ptr(re), _ptr(im), re.shape[0], re.shape[1], _ptr(out))
+    return out
+
+
+def reconstruct_fourier(geom, rot_start, det_start, sino, angles, nx, ny, interp, zeropad):
+    """The GUI's Fourier reconstruction: convertFFTPolar, ifft, magnitude, shuffle."""
+    re, im, _ = convert_fft_polar(geom, rot_start, det_start, sino, angles, nx, ny, interp, zeropad)
+    return ifft_magnitude(re, im)

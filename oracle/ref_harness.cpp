@@ -15,6 +15,9 @@
 //       private image per thread, images summed: src/threadrecon.cpp:176-255)
 //   ref_harness rebin   IN.pj OUT.pj
 //       Projections::interpolateToParallel (libctsim/projections.cpp:1250-1328)
+//   ref_harness polar   PJFILE NX NY INTERP out.f32
+//       Projections::convertPolar (libctsim/projections.cpp:953-995) into a
+//       cleared FP32 ImageFile, dumped column-major
 //   ref_harness comp    A.if B.if
 //       ImageFile::comparativeStatistics (libctsim/imagefile.cpp:186-240),
 //       printed as "d r e" with 17 significant digits
@@ -158,6 +161,21 @@ static int cmdRebin(int argc, char** argv) {
   return ok ? 0 : 2;
 }
 
+static int cmdPolar(int argc, char** argv) {
+  if (argc < 7) return 2;
+  Projections pj;
+  if (!pj.read(argv[2])) { fprintf(stderr, "pj read fail\n"); return 2; }
+  int nx = atoi(argv[3]), ny = atoi(argv[4]);
+  ImageFile im(nx, ny);
+  im.arrayDataClear();
+  if (!pj.convertPolar(im, Projections::convertInterpNameToID(argv[5]))) return 3;
+  std::vector<float> out((size_t)nx * ny);
+  ImageFileArray v = im.getArray();
+  for (int ix = 0; ix < nx; ix++)
+    for (int iy = 0; iy < ny; iy++) out[(size_t)ix * ny + iy] = v[ix][iy];
+  return writeRaw(argv[6], out.data(), out.size() * 4) ? 0 : 2;
+}
+
 static int cmdComp(int argc, char** argv) {
   if (argc < 4) return 2;
   ImageFile a, b;
@@ -169,7 +187,7 @@ static int cmdComp(int argc, char** argv) {
 }
 
 int main(int argc, char** argv) {
-  if (argc < 2) { fprintf(stderr, "usage: ref_harness filter|bp|timerec|timeraysum|rebin|comp ...\n"); return 2; }
+  if (argc < 2) { fprintf(stderr, "usage: ref_harness filter|bp|timerec|timeraysum|rebin|comp|polar ...\n"); return 2; }
   std::string c = argv[1];
   if (c == "filter") return cmdFilter(argc, argv);
   if (c == "bp") return cmdBackproject(argc, argv);
@@ -177,6 +195,7 @@ int main(int argc, char** argv) {
   if (c == "timeraysum") return cmdTimeRaysum(argc, argv);
   if (c == "rebin") return cmdRebin(argc, argv);
   if (c == "comp") return cmdComp(argc, argv);
+  if (c == "polar") return cmdPolar(argc, argv);
   fprintf(stderr, "unknown command %s\n", argv[1]);
   return 2;
 }

@@ -220,6 +220,29 @@ def make_io(tmp):
     np.savez_compressed(os.path.join(HERE, "io.npz"), **out)
 
 
+# Projections::convertPolar of reference scans (ref_harness polar)
+POLARS = [("herman_par", 48, 48, "nearest"), ("herman_par", 48, 48, "bilinear"),
+          ("shepp_par_even", 40, 32, "bilinear"), ("shepp_par_even", 33, 33, "nearest"),
+          ("shepp_eqa", 36, 36, "bilinear"), ("shepp_eqa_even", 30, 30, "nearest"),
+          ("herman_eql", 30, 30, "bilinear")]
+
+
+def make_polar(tmp):
+    out = {}
+    for k, (name, nx, ny, interp) in enumerate(POLARS):
+        pjf = os.path.join(tmp, name + ".pj")
+        if not os.path.exists(pjf):
+            sc = [s for s in SCANS if s[0] == name][0]
+            run(REF, "phm2pj", pjf, sc[3], sc[4], "--phantom", sc[1], "--geometry", sc[2],
+                "--nray", sc[5], *sc[6])
+        f = os.path.join(tmp, "polar.f32")
+        run(HARN, "polar", pjf, nx, ny, interp, f)
+        out["%d/image" % k] = np.fromfile(f, np.float32).reshape(nx, ny)
+        out.update(pj_arrays("%d/" % k, read_pj(pjf)))
+        out["%d/cfg" % k] = np.array([name, nx, ny, interp], dtype=object)
+    np.savez_compressed(os.path.join(HERE, "polar.npz"), **out)
+
+
 def main():
     for b in (REF, REF64, HARN):
         if not os.path.exists(b):
@@ -238,6 +261,8 @@ def main():
             make_raster(tmp)
         if not only or "io" in only:
             make_io(tmp)
+        if not only or "polar" in only:
+            make_polar(tmp)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print("%-14s %8d bytes" % (f, os.path.getsize(os.path.join(HERE, f))))
