@@ -451,6 +451,49 @@ def files_io(args, torch, cg, device, sinos, angles, images, B):
     }
 
 
+def fourier_recon(args, torch, cg, device, sinos, g, angles, B):
+    """The direct-Fourier path on the main workload's equiangular scans:
+    rebinning to parallel rays, convertFFTPolar (N = 1024), the inverse 2-D
+    transform with magnitude, per 512 x 512 image; convertPolar alone; the
+    oracle's restatement of one image on the host as the CPU figure."""
+    import sys as _sys
+    n = min(B, 8)
+    out = torch.empty((NX, NX), dtype=torch.float32, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timed(fn):
+        fn(0)
+        torch.cuda.synchronize()
+        ev[0].record()
+        for b in range(n):
+            fn(b)
+        ev[1].record()
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[1]) / n
+
+    rec_ms = timed(lambda b: out.copy_(device.reconstruct_fourier(g, sinos[b], angles, NX, NX,
+                                                                   "bilinear", 1)))
+    pol_ms = timed(lambda b: device.convert_polar(g, sinos[b], angles, NX, NX, "bilinear"))
+    _sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    og = po.Geom(g.geometry, g.n_det, g.n_view, g.rot_inc, g.det_inc, g.focal_length,
+                 g.source_detector_length, g.view_diameter, g.fan_beam_angle)
+    data = sinos[0, :, :N_DET].cpu().numpy()
+    t0 = time.perf_counter()
+    ref = po.reconstruct_fourier(og, g.rot_start, g.det_start, data, angles, NX, NX, "bilinear", 1)
+    cpu_s = time.perf_counter() - t0
+    got = device.reconstruct_fourier(g, sinos[0], angles, NX, NX, "bilinear", 1).cpu().numpy()
+    err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    return {"workload": "733 x 720 equiangular -> parallel -> 512 x 512, bilinear, zeropad 1 "
+                        "(transform length 1024)",
+            "reconstruct_fourier_ms_per_image": rec_ms, "images_per_s": 1e3 / rec_ms,
+            "convert_polar_ms_per_image": pol_ms,
+            "rel_l2_vs_fp64_oracle": err,
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "images/s", "cores": 1,
+                             "kind": "port", "sample": "one image, FP64 restatement "
+                             "(radix-2 FFTs)"}}
+
+
 def chunks(b):
     """slice chunks of ctgpu_recon_run_batch_host: 8, 24, then 32"""
     out, nxt = [], 8
@@ -562,6 +605,8 @@ def run_gpu(args):
         if args.batched_problems > 0 else None
     helical = helical_3d(args, torch, cg, device, phantoms, rank) if args.helical else None
     files = files_io(args, torch, cg, device, sinos, angles[0], images, B) if args.files else None
+    fourier = fourier_recon(args, torch, cg, device, sinos, g, angles[0], B) \
+        if args.fourier else None
 
     if rank != 0:
         return 0
@@ -622,6 +667,7 @@ def run_gpu(args):
         "batched_uneven": batched,
         "helical": helical,
         "files": files,
+        "fourier": fourier,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))
@@ -641,6 +687,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--helical", type=int, default=1,
                     help="measure the helical 3-D workload after the main one (0: skip)")
+    ap.add_argument("--fourier", type=int, default=1,
+                    help="measure the direct-Fourier reconstruction after the main workload "
+                         "(0: skip)")
     ap.add_argument("--files", type=int, default=1,
                     help="measure the device-resident file I/O after the main workload (0: skip)")
     ap.add_argument("--batched-problems", type=int, default=64,
