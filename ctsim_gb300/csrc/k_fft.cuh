@@ -4,6 +4,12 @@
 // registers, synchronises, and writes them back in the next pass's order;
 // twiddles come from an FP64-computed table tw[m] = exp(-2 pi i m / N).
 // All threads of the block take part; blockDim >= N / 16.
+//
+// Element m of the sequence lives at buf[fpad(m)], its low four index bits
+// XORed with bits 3-6 (a permutation within each block of 16 elements): every
+// pass's reads and writes of a half-warp then fall on 16 different bank pairs
+// (the first pass writes with a stride of 8 elements, which would otherwise
+// hit two).  Shared memory: fft_smem_elems(N) float2.
 #pragma once
 
 #include "ctgpu_internal.h"
@@ -62,13 +68,17 @@ __device__ __forceinline__ void dft(float2 (&u)[R]) {
   }
 }
 
+__host__ __device__ __forceinline__ int fpad(int m) { return m ^ ((m >> 3) & 15); }
+__host__ __device__ __forceinline__ int fft_smem_elems(int n) { return (n + 15) & ~15; }
+
 // One Stockham pass of radix R over buf[N] (p = product of the radices done):
 // butterfly i takes x[i + r N/R], twiddles by W^(r k N/(pR)) with k = i mod p,
 // and writes y[(i - k) R + k + r p].
-template <int R>
+// M = N / (8 blockDim) (1 or 2): butterflies per thread M * 8 / R.
+template <int R, int M>
 __device__ __forceinline__ void stockham_pass(float2* buf, int N, int p,
                                               const float2* __restrict__ tw) {
-  constexpr int SMAX = 16 / R;   // butterflies per thread (blockDim >= N / 8)
+  constexpr int SMAX = M * 8 / R;
   const int nb = N / R, T = blockDim.x, stride = N / (p * R);
   float2 u[SMAX][R];
 #pragma unroll
@@ -78,7 +88,7 @@ __device__ __forceinline__ void stockham_pass(float2* buf, int N, int p,
       const int k = i & (p - 1);
 #pragma unroll
       for (int r = 0; r < R; r++) {
-        float2 v = buf[i + r * nb];
+        float2 v = buf[fpad(i + r * nb)];
         if (r > 0 && k > 0) v = cmul(v, __ldg(&tw[r * k * stride]));
         u[s][r] = v;
       }
@@ -93,20 +103,27 @@ __device__ __forceinline__ void stockham_pass(float2* buf, int N, int p,
       dft<R>(u[s]);
       const int j = (i - k) * R + k;
 #pragma unroll
-      for (int r = 0; r < R; r++) buf[j + r * p] = u[s][r];
+      for (int r = 0; r < R; r++) buf[fpad(j + r * p)] = u[s][r];
     }
   }
   __syncthreads();
 }
 
-__device__ void fft_forward(float2* buf, int N, const float2* __restrict__ tw) {
+template <int M>
+__device__ void fft_forward_m(float2* buf, int N, const float2* __restrict__ tw) {
   int p = 1;
   while (p * 8 <= N) {
-    stockham_pass<8>(buf, N, p, tw);
+    stockham_pass<8, M>(buf, N, p, tw);
     p *= 8;
   }
-  if (p * 4 == N) stockham_pass<4>(buf, N, p, tw);
-  else if (p * 2 == N) stockham_pass<2>(buf, N, p, tw);
+  if (p * 4 == N) stockham_pass<4, M>(buf, N, p, tw);
+  else if (p * 2 == N) stockham_pass<2, M>(buf, N, p, tw);
+}
+
+// forward transform of buf (padded layout); blockDim >= N / 16
+__device__ __forceinline__ void fft_forward(float2* buf, int N, const float2* __restrict__ tw) {
+  if ((int)blockDim.x * 8 >= N) fft_forward_m<1>(buf, N, tw);
+  else fft_forward_m<2>(buf, N, tw);
 }
 
 }  // namespace

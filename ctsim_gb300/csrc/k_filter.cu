@@ -23,13 +23,17 @@
 
 namespace ctgpu {
 
+// M = N / (8 blockDim): 1 up to N = 8192, 2 for N = 16384 (a template
+// parameter, so that each kernel holds only the registers its passes use)
+template <int M>
 __global__ void __launch_bounds__(1024) fft_filter_kernel(FilterLaunch L) {
-  extern __shared__ float2 zb[];
+  extern __shared__ float2 zb[];   // swizzled: element m at zb[fpad(m)]
   const int N = L.fftN, n = L.nDet;
   const int v0 = 2 * blockIdx.x;
   const bool two = v0 + 1 < L.nViews;
   const float* ia = L.in + (size_t)blockIdx.y * L.inSliceStride + (size_t)v0 * L.inPitch;
   const float* ib = ia + L.inPitch;
+#pragma unroll 4
   for (int m = threadIdx.x; m < N; m += blockDim.x) {
     float2 v = make_float2(0.f, 0.f);
     if (m < n) {
@@ -37,22 +41,22 @@ __global__ void __launch_bounds__(1024) fft_filter_kernel(FilterLaunch L) {
       v.x = w * ia[m];
       if (two) v.y = w * ib[m];
     }
-    zb[m] = v;
+    zb[fpad(m)] = v;
   }
   __syncthreads();
-  fft_forward(zb, N, L.twiddle);
+  fft_forward_m<M>(zb, N, L.twiddle);
   // multiply by the kernel's spectrum; conjugate, so that the forward
   // transform below is the inverse one
   for (int m = threadIdx.x; m < N; m += blockDim.x) {
-    const float2 z = cmul(zb[m], __ldg(&L.spectrum[m]));
-    zb[m] = make_float2(z.x, -z.y);
+    const float2 z = cmul(zb[fpad(m)], __ldg(&L.spectrum[m]));
+    zb[fpad(m)] = make_float2(z.x, -z.y);
   }
   __syncthreads();
-  fft_forward(zb, N, L.twiddle);
+  fft_forward_m<M>(zb, N, L.twiddle);
   float* oa = L.out + (size_t)blockIdx.y * L.outSliceStride + (size_t)v0 * L.outPitch;
   float* ob = oa + L.outPitch;
   for (int m = threadIdx.x; m < n; m += blockDim.x) {
-    const float2 y = zb[m];
+    const float2 y = zb[fpad(m)];
     oa[m] = y.x;
     if (two) ob[m] = -y.y;
   }
@@ -62,19 +66,23 @@ cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s) {
   if (L.nViews <= 0) return cudaSuccess;
   const int N = L.fftN;
   if (N < 4 || (N & (N - 1)) || N > 16384 || N < 2 * L.nDet - 1) return cudaErrorInvalidValue;
-  const size_t smem = sizeof(float2) * (size_t)N;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(fft_filter_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
+  const size_t smem = sizeof(float2) * (size_t)fft_smem_elems(N);
   int T = N / 8;
   if (T < 32) T = 32;
   if (T > 1024) T = 1024;
+  const bool one = T * 8 >= N;
+  if (smem > 48 * 1024) {
+    cudaError_t e = one ? cudaFuncSetAttribute(fft_filter_kernel<1>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                        : cudaFuncSetAttribute(fft_filter_kernel<2>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   const int nBatch = L.nBatch > 0 ? L.nBatch : 1;
   if (nBatch > 65535) return cudaErrorInvalidConfiguration;
   dim3 grid((L.nViews + 1) / 2, nBatch);
-  fft_filter_kernel<<<grid, T, smem, s>>>(L);
+  if (one) fft_filter_kernel<1><<<grid, T, smem, s>>>(L);
+  else fft_filter_kernel<2><<<grid, T, smem, s>>>(L);
   return cudaGetLastError();
 }
 

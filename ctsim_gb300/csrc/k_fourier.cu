@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(256) polar_kernel(PolarLaunch L) {
   if (L.outIm) L.outIm[o] = (float)vi;
 }
 
-// direct DFT of z[n] (sign -1 forward, +1 backward) into out[n], shared memory
+// direct DFT of z (swizzled layout, element j at z[fpad(j)]; sign -1 forward,
+// +1 backward) into out[n] (plain layout), shared memory
 __device__ void dft_direct(const float2* z, float2* out, int n, const float2* __restrict__ tw,
                            int sign) {
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
@@ -130,8 +131,9 @@ __device__ void dft_direct(const float2* z, float2* out, int n, const float2* __
     for (int j = 0; j < n; j++) {
       const float2 w = __ldg(&tw[idx]);
       const float wi = sign < 0 ? w.y : -w.y;
-      sr = fmaf(z[j].x, w.x, fmaf(-z[j].y, wi, sr));
-      si = fmaf(z[j].x, wi, fmaf(z[j].y, w.x, si));
+      const float2 zj = z[fpad(j)];
+      sr = fmaf(zj.x, w.x, fmaf(-zj.y, wi, sr));
+      si = fmaf(zj.x, wi, fmaf(zj.y, w.x, si));
       idx += k;
       if (idx >= n) idx -= n;
     }
@@ -139,23 +141,24 @@ __device__ void dft_direct(const float2* z, float2* out, int n, const float2* __
   }
 }
 
-// transform buf[n] in place (pow2: Stockham; else direct DFT through tmp)
+// transform buf (swizzled layout) in place (pow2: Stockham; else direct DFT
+// through tmp)
 __device__ __forceinline__ void line_transform(float2* buf, float2* tmp, int n,
                                                const float2* __restrict__ tw, int sign) {
   if ((n & (n - 1)) == 0) {
     if (sign > 0)   // backward = conj(forward(conj))
-      for (int m = threadIdx.x; m < n; m += blockDim.x) buf[m].y = -buf[m].y;
+      for (int m = threadIdx.x; m < n; m += blockDim.x) buf[fpad(m)].y = -buf[fpad(m)].y;
     __syncthreads();
     if (n > 1) fft_forward(buf, n, tw);
     if (sign > 0) {
-      for (int m = threadIdx.x; m < n; m += blockDim.x) buf[m].y = -buf[m].y;
+      for (int m = threadIdx.x; m < n; m += blockDim.x) buf[fpad(m)].y = -buf[fpad(m)].y;
       __syncthreads();
     }
   } else {
     __syncthreads();
     dft_direct(buf, tmp, n, tw, sign);
     __syncthreads();
-    for (int m = threadIdx.x; m < n; m += blockDim.x) buf[m] = tmp[m];
+    for (int m = threadIdx.x; m < n; m += blockDim.x) buf[fpad(m)] = tmp[m];
     __syncthreads();
   }
 }
@@ -163,8 +166,8 @@ __device__ __forceinline__ void line_transform(float2* buf, float2* tmp, int n,
 // one CTA per view: convertFFTPolar's per-view steps (projections.cpp:1034-1067)
 __global__ void __launch_bounds__(1024) fourier_views_kernel(FourierViewsLaunch L) {
   extern __shared__ float2 zs[];
-  float2* buf = zs;
-  float2* tmp = zs + L.N;
+  float2* buf = zs;                          // swizzled layout
+  float2* tmp = zs + fft_smem_elems(L.N);    // direct DFT only
   const int v = blockIdx.x, N = L.N, nI = L.nInterp, nDet = L.nDet;
   const float* row = L.sino + (size_t)v * L.pitch;
   const int zeros = N - nI;
@@ -191,14 +194,14 @@ __global__ void __launch_bounds__(1024) fourier_views_kernel(FourierViewsLaunch 
       }
       val.x = (float)(r * L.projScale);
     }
-    buf[m] = val;
+    buf[fpad(m)] = val;
   }
   __syncthreads();
   line_transform(buf, tmp, N, L.twiddle, -1);
   float2* out = L.spec + (size_t)v * N;
   const float sc = (float)L.fftScale;
   for (int d = threadIdx.x; d < N; d += blockDim.x) {
-    const float2 z = buf[nat_src(N, d)];
+    const float2 z = buf[fpad(nat_src(N, d))];
     out[d] = make_float2(z.x * sc, z.y * sc);
   }
 }
@@ -210,26 +213,26 @@ __global__ void __launch_bounds__(1024) ifft_lines_kernel(IfftLaunch L, int pass
   extern __shared__ float2 zs[];
   const int nx = L.nx, ny = L.ny;
   const int n = pass == 1 ? ny : nx;
-  float2* buf = zs;
-  float2* tmp = zs + n;
+  float2* buf = zs;                      // swizzled layout
+  float2* tmp = zs + fft_smem_elems(n);   // direct DFT only
   const int line = blockIdx.x;
   if (pass == 1) {
     const int sx = fou_src(nx, line);
     for (int m = threadIdx.x; m < ny; m += blockDim.x) {
       const size_t s = (size_t)sx * ny + fou_src(ny, m);
-      buf[m] = make_float2(L.inRe[s], L.inIm[s]);
+      buf[fpad(m)] = make_float2(L.inRe[s], L.inIm[s]);
     }
   } else {
     const int k2 = nat_src(ny, line);   // this CTA writes output row `line`
-    for (int m = threadIdx.x; m < nx; m += blockDim.x) buf[m] = L.tmp[(size_t)m * ny + k2];
+    for (int m = threadIdx.x; m < nx; m += blockDim.x) buf[fpad(m)] = L.tmp[(size_t)m * ny + k2];
   }
   __syncthreads();
   line_transform(buf, tmp, n, pass == 1 ? L.twY : L.twX, +1);
   if (pass == 1) {
-    for (int m = threadIdx.x; m < ny; m += blockDim.x) L.tmp[(size_t)line * ny + m] = buf[m];
+    for (int m = threadIdx.x; m < ny; m += blockDim.x) L.tmp[(size_t)line * ny + m] = buf[fpad(m)];
   } else {
     for (int d1 = threadIdx.x; d1 < nx; d1 += blockDim.x) {
-      const float2 z = buf[nat_src(nx, d1)];   // the reference keeps FP32 re / im
+      const float2 z = buf[fpad(nat_src(nx, d1))];   // the reference keeps FP32 re / im
       const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(z.x, z.x), __fmul_rn(z.y, z.y)));
       L.out[(size_t)d1 * ny + line] = mag;
     }
@@ -254,7 +257,7 @@ cudaError_t launch_polar(const PolarLaunch& L, cudaStream_t s) {
 }
 
 size_t line_smem_bytes(int n) {
-  return sizeof(float2) * (size_t)n * (((n & (n - 1)) == 0) ? 1 : 2);
+  return sizeof(float2) * ((size_t)fft_smem_elems(n) + (((n & (n - 1)) == 0) ? 0 : (size_t)n));
 }
 
 cudaError_t launch_fourier_views(const FourierViewsLaunch& L, cudaStream_t s) {
