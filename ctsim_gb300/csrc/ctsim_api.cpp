@@ -263,20 +263,119 @@ bool Projections::write(const char* fn) {   // projections.cpp:485-546, :780-889
 }
 
 void Projections::printScanInfo(std::string& out) const {
-  std::ostringstream os;   // projections.cpp printScanInfo
+  std::ostringstream os;   // projections.cpp:935-949
   os << "Number of detectors: " << m_g.n_det << "\n";
-  os << "    Number of views: " << m_g.n_view << "\n";
-  os << "             Remark: " << m_remark << "\n";
-  os << "           Geometry: " << Scanner::convertGeometryIDToName(m_g.geometry) << "\n";
-  os << "       Focal Length: " << m_g.focal_length << "\n";
-  os << "    Source Detector Length: " << m_g.source_detector_length << "\n";
-  os << "      View Diameter: " << m_g.view_diameter << "\n";
-  os << "     Fan Beam Angle: " << m_g.fan_beam_angle << "\n";
-  os << "           detStart: " << m_g.det_start << "\n";
-  os << "             detInc: " << m_g.det_inc << "\n";
-  os << "           rotStart: " << m_g.rot_start << "\n";
-  os << "             rotInc: " << m_g.rot_inc << "\n";
+  os << "Number of views: " << m_g.n_view << "\n";
+  os << "Description: " << m_remark.c_str() << "\n";
+  os << "Geometry: " << Scanner::convertGeometryIDToName(m_g.geometry) << "\n";
+  os << "Focal Length: " << m_g.focal_length << "\n";
+  os << "Source Detector Length: " << m_g.source_detector_length << "\n";
+  os << "View Diameter: " << m_g.view_diameter << "\n";
+  os << "Fan Beam Angle: " << m_g.fan_beam_angle * (180. / 3.14159265358979323846) << "\n";
+  os << "detStart: " << m_g.det_start << "\n";
+  os << "detInc: " << m_g.det_inc << "\n";
+  os << "rotStart: " << m_g.rot_start << "\n";
+  os << "rotInc: " << m_g.rot_inc << "\n";
   out = os.str();
+}
+
+void Projections::printProjectionData(int startView, int endView) const {
+  std::printf("Projections Data\n\n");   // projections.cpp:905-932
+  std::printf("Description: %s\n", m_remark.c_str());
+  std::printf("Geometry: %s\n", Scanner::convertGeometryIDToName(m_g.geometry));
+  std::printf("nView       = %8d             nDet = %8d\n", m_g.n_view, m_g.n_det);
+  std::printf("focalLength = %8.4f   ViewDiameter = %8.4f\n", m_g.focal_length, m_g.view_diameter);
+  std::printf("fanBeamAngle= %8.4f SourceDetector = %8.4f\n",
+              m_g.fan_beam_angle * (180. / 3.14159265358979323846), m_g.source_detector_length);
+  std::printf("rotStart    = %8.4f         rotInc = %8.4f\n", m_g.rot_start, m_g.rot_inc);
+  std::printf("detStart    = %8.4f         detInc = %8.4f\n", m_g.det_start, m_g.det_inc);
+  if (m_views.empty()) return;
+  const int nView = m_g.n_view;
+  if (startView < 0) startView = 0;
+  if (endView < 0) endView = nView - 1;
+  if (startView > nView - 1) startView = nView - 1;
+  if (endView > nView - 1) endView = nView - 1;
+  for (int ir = startView; ir <= endView - 1; ir++) {   // the reference stops one short
+    std::printf("View %d: angle %f\n", ir, m_views[ir].viewAngle());
+    const DetectorValue* v = m_views[ir].detValues();
+    for (int id = 0; id < m_g.n_det; id++) std::printf("%8.4f  ", v[id]);
+    std::printf("\n");
+  }
+}
+
+bool Projections::copyHeader(const char* fn, std::ostream& os) {
+  std::vector<char> b;
+  if (!slurp(fn, b) || b.size() < 4) return false;
+  uint16_t hs, sig;
+  std::memcpy(&hs, b.data(), 2);
+  std::memcpy(&sig, b.data() + 2, 2);
+  if (sig != 'P' * 256 + 'J') {
+    std::fprintf(stderr, "Illegal signature in projection file %s\n", fn);
+    return false;
+  }
+  if (hs > b.size()) return false;
+  os.write(b.data(), hs);
+  return (bool)os;
+}
+
+bool Projections::copyViewData(const char* fn, std::ostream& os, int startView, int endView) {
+  std::vector<char> b;
+  if (!slurp(fn, b) || b.size() < 12) {
+    std::fprintf(stderr, "Unable to read projection file %s\n", fn);
+    return false;
+  }
+  uint16_t hs, sig;
+  uint32_t nv, nd;
+  std::memcpy(&hs, b.data(), 2);
+  std::memcpy(&sig, b.data() + 2, 2);
+  std::memcpy(&nv, b.data() + 4, 4);
+  std::memcpy(&nd, b.data() + 8, 4);
+  if (sig != 'P' * 256 + 'J') {
+    std::fprintf(stderr, "Illegal signature in projection file %s\n", fn);
+    return false;
+  }
+  const int nView = (int)nv;   // projections.cpp:706-717
+  if (startView < 0) startView = 0;
+  if (startView > nView - 1) startView = nView;
+  if (endView < 0 || endView > nView - 1) endView = nView - 1;
+  if (startView > endView) std::swap(startView, endView);
+  const size_t sizeView = 12 + 4 * (size_t)nd;
+  for (int i = startView; i <= endView; i++) {
+    const size_t off = hs + (size_t)i * sizeView;
+    if (off + sizeView > b.size()) {
+      std::fprintf(stderr, "Error reading projection file\n");
+      return false;
+    }
+    os.write(b.data() + off, sizeView);
+    if (!os) return false;
+  }
+  return true;
+}
+
+int Projections::convertInterpNameToID(const char* name) {   // projections.cpp:36-50, 90-101
+  if (name && !strcasecmp(name, "nearest")) return 0;
+  if (name && !strcasecmp(name, "bilinear")) return 1;
+  return -1;
+}
+
+bool Projections::convertPolar(ImageFile& im, int interpID) const {
+  if (im.nx() == 0 || im.ny() == 0 || m_views.empty()) return false;
+  const char* name = interpID == 0 ? "nearest" : interpID == 1 ? "bilinear" : nullptr;
+  if (!name) return true;   // the reference's interpolatePolar writes nothing then
+  const size_t rows = sizeof(float) * (size_t)m_g.n_view * m_pitch;
+  float *dS = nullptr, *dI = nullptr;
+  bool ok = cudaMalloc(&dS, rows) == cudaSuccess &&
+            cudaMalloc(&dI, sizeof(float) * (size_t)im.nx() * im.ny()) == cudaSuccess &&
+            cudaMemcpy(dS, m_data.data(), rows, cudaMemcpyHostToDevice) == cudaSuccess;
+  std::vector<double> ang = viewAngles();
+  if (ok) ok = ctgpu_convert_polar(&m_g, dS, m_pitch, ang.data(), im.nx(), im.ny(), name, dI,
+                                   nullptr) == CTGPU_OK;
+  if (ok) ok = cudaMemcpy(im.data(), dI, sizeof(float) * (size_t)im.nx() * im.ny(),
+                          cudaMemcpyDeviceToHost) == cudaSuccess;
+  if (!ok) std::fprintf(stderr, "%s\n", ctgpu_last_error());
+  cudaFree(dS);
+  cudaFree(dI);
+  return ok;
 }
 
 static int helical_status(const std::string& msg) {
@@ -482,7 +581,103 @@ bool ImageFile::fileRead(const char* fn) {
     if (ps == 4) { float v; std::memcpy(&v, b.data() + off + 4 * i, 4); m_data[i] = v; }
     else { double v; std::memcpy(&v, b.data() + off + 8 * i, 8); m_data[i] = (float)v; }
   }
+  // labels after the real (and imaginary) planes (array2dfile.cpp:559-595)
+  m_labels.clear();
+  size_t lo = off + n * ps * (dt == 2 ? 2 : 1);
+  for (int i = 0; i < nl; i++) {
+    uint16_t h[7], len;
+    double ct;
+    if (lo + 24 > b.size()) break;
+    std::memcpy(h, b.data() + lo, 14);
+    std::memcpy(&ct, b.data() + lo + 14, 8);
+    std::memcpy(&len, b.data() + lo + 22, 2);
+    if (lo + 24 + len > b.size()) break;
+    Label l;
+    l.type = h[0];
+    for (int j = 0; j < 6; j++) l.date[j] = h[1 + j];
+    l.calcTime = ct;
+    l.text.assign(b.data() + lo + 24, len);
+    m_labels.push_back(l);
+    lo += 24 + len;
+  }
   return true;
+}
+
+// device-backed comparison and arithmetic of real images
+namespace {
+struct DevImages {
+  float* p[3] = {nullptr, nullptr, nullptr};
+  ~DevImages() {
+    for (float* q : p)
+      if (q) cudaFree(q);
+  }
+};
+}  // namespace
+
+bool ImageFile::comparativeStatistics(const ImageFile& c, double& d, double& r, double& e) const {
+  // imagefile.cpp:188-191: the reference rejects only when both sizes differ
+  // (and then reads past the smaller image); both must match here
+  if (c.nx() != m_nx || c.ny() != m_ny) {
+    std::fprintf(stderr, "Image sizes differ [ImageFile::comparativeStatistics]\n");
+    return false;
+  }
+  if (m_nx == 0 || m_ny == 0) return false;
+  const size_t n = (size_t)m_nx * m_ny;
+  DevImages dv;
+  double dre[3];
+  bool ok = cudaMalloc(&dv.p[0], 4 * n) == cudaSuccess && cudaMalloc(&dv.p[1], 4 * n) == cudaSuccess &&
+            cudaMemcpy(dv.p[0], m_data.data(), 4 * n, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(dv.p[1], c.m_data.data(), 4 * n, cudaMemcpyHostToDevice) == cudaSuccess &&
+            ctgpu_image_compare(dv.p[0], dv.p[1], 1, m_nx, m_ny, n, dre, nullptr) == CTGPU_OK;
+  if (!ok) return false;
+  d = dre[0];
+  r = dre[1];
+  e = dre[2];
+  return true;
+}
+
+bool ImageFile::printComparativeStatistics(const ImageFile& c, std::ostream& os) const {
+  double d, r, e;   // imagefile.cpp:243-256
+  if (!comparativeStatistics(c, d, r, e)) return false;
+  os << "  Normalized root mean squared distance (d): " << d << std::endl;
+  os << "      Normalized mean absolute distance (r): " << r << std::endl;
+  os << "Worst case distance (2x2 pixel average) (e): " << e << std::endl;
+  return true;
+}
+
+bool ImageFile::arith(const char* op, const ImageFile& b, ImageFile& out) const {
+  if (m_nx != b.nx() || m_ny != b.ny() || m_nx != out.nx() || m_ny != out.ny()) {
+    std::fprintf(stderr, "Difference sizes of images [ImageFile::%s]\n", op);
+    return false;
+  }
+  const size_t n = (size_t)m_nx * m_ny;
+  if (!n) return true;
+  DevImages dv;
+  bool ok = cudaMalloc(&dv.p[0], 4 * n) == cudaSuccess && cudaMalloc(&dv.p[1], 4 * n) == cudaSuccess &&
+            cudaMalloc(&dv.p[2], 4 * n) == cudaSuccess &&
+            cudaMemcpy(dv.p[0], m_data.data(), 4 * n, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(dv.p[1], b.m_data.data(), 4 * n, cudaMemcpyHostToDevice) == cudaSuccess &&
+            ctgpu_image_arith(op, dv.p[0], dv.p[1], dv.p[2], n, nullptr) == CTGPU_OK &&
+            cudaMemcpy(out.data(), dv.p[2], 4 * n, cudaMemcpyDeviceToHost) == cudaSuccess;
+  return ok;
+}
+bool ImageFile::addImages(const ImageFile& b, ImageFile& out) const { return arith("add", b, out); }
+bool ImageFile::subtractImages(const ImageFile& b, ImageFile& out) const {
+  return arith("subtract", b, out);
+}
+bool ImageFile::multiplyImages(const ImageFile& b, ImageFile& out) const {
+  return arith("multiply", b, out);
+}
+bool ImageFile::divideImages(const ImageFile& b, ImageFile& out) const {
+  return arith("divide", b, out);
+}
+
+void ImageFile::labelsCopy(const ImageFile& f, const char* id) {
+  for (const Label& l : f.m_labels) {
+    Label c = l;
+    c.text = std::string(id ? id : "") + l.text;
+    m_labels.push_back(c);
+  }
 }
 
 // ========================================================== ProcessSignal ==

@@ -441,19 +441,77 @@ int phm2if_main(int argc, char* const argv[]) {
 }
 
 // ------------------------------------------------------------------ pjinfo --
-int pjinfo_main(int argc, char* const argv[]) {
-  if (argc < 2) {
-    std::cout << "usage: " << base_name(argv[0]) << " projection-file\n";
-    return 1;
+void pjinfo_usage(const char* program) {
+  std::cout << "usage: " << base_name(program) << " proj-file [OPTIONS]\n";
+  std::cout << "Display projection file information\n\n";
+  std::cout << "   --binaryheader  Dump binary header data\n";
+  std::cout << "   --binaryviews   Dump binary view data\n";
+  std::cout << "   --startview n   Beginning view number to display (default=0)\n";
+  std::cout << "   --endview n     Ending view number to display (default=last view)\n";
+  std::cout << "   --dump          Print all scan data ASCII format\n";
+  std::cout << "   --version       Print version\n";
+  std::cout << "   --help          Print this help message\n";
+}
+
+int pjinfo_main(int argc, char* const argv[]) {   // tools/pjinfo.cpp:33-151
+  enum { O_BINARYHEADER, O_BINARYVIEWS, O_STARTVIEW, O_ENDVIEW, O_DUMP, O_HELP, O_VERSION };
+  const struct option options[] = {{"binaryheader", 0, 0, O_BINARYHEADER},
+                                   {"binaryviews", 0, 0, O_BINARYVIEWS},
+                                   {"startview", 1, 0, O_STARTVIEW},
+                                   {"endview", 1, 0, O_ENDVIEW},
+                                   {"dump", 0, 0, O_DUMP},
+                                   {"help", 0, 0, O_HELP},
+                                   {"version", 0, 0, O_VERSION},
+                                   {0, 0, 0, 0}};
+  bool dump = false, binHeader = false, binViews = false;
+  int startView = 0, endView = -1;
+  optind = 0;
+  while (1) {
+    int c = getopt_long(argc, argv, "", options, nullptr);
+    if (c == -1) break;
+    switch (c) {
+      case O_DUMP: dump = true; break;
+      case O_BINARYHEADER: binHeader = true; break;
+      case O_BINARYVIEWS: binViews = true; break;
+      case O_STARTVIEW:
+        if (!parse_int(optarg, startView)) {
+          std::cerr << "Error setting --startview to %s" << optarg << std::endl;
+          pjinfo_usage(argv[0]);
+          return 1;
+        }
+        break;
+      case O_ENDVIEW:
+        if (!parse_int(optarg, endView)) {
+          std::cerr << "Error setting --endview to %s" << optarg << std::endl;
+          pjinfo_usage(argv[0]);
+          return 1;
+        }
+        break;
+      case O_VERSION: std::cout << "Version 5.2.0 (GB300)" << std::endl; return 0;
+      case O_HELP: case '?': pjinfo_usage(argv[0]); return 0;
+      default: pjinfo_usage(argv[0]); return 1;
+    }
   }
-  Projections pj;
-  if (!pj.read(argv[argc - 1])) {
-    std::cerr << "Error reading " << argv[argc - 1] << std::endl;
-    return 1;
+  if (argc - optind != 1) { pjinfo_usage(argv[0]); return 1; }
+  const char* name = argv[optind];
+  if (binHeader) {
+    Projections::copyHeader(name, std::cout);
+  } else if (binViews) {
+    Projections::copyViewData(name, std::cout, startView, endView);
+  } else {
+    Projections pj;
+    if (!pj.read(name)) {
+      std::cerr << "Can not open projection file " << name << std::endl;
+      return 1;
+    }
+    if (dump) {
+      pj.printProjectionData(startView, endView);
+    } else {
+      std::string info;
+      pj.printScanInfo(info);
+      std::cout << info;
+    }
   }
-  std::string info;
-  pj.printScanInfo(info);
-  std::cout << info;
   return 0;
 }
 

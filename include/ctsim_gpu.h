@@ -21,6 +21,7 @@
 #ifndef CTSIM_GPU_H
 #define CTSIM_GPU_H
 
+#include <ostream>
 #include <string>
 #include <vector>
 
@@ -168,6 +169,16 @@ class Projections {
   double calcTime() const { return m_calcTime; }
   void setCalcTime(double t) { m_calcTime = t; }
   void printScanInfo(std::string& out) const;
+  // projections.cpp:899-932, pjinfo --dump (prints views start .. end-1, as there)
+  void printProjectionData(int startView, int endView) const;
+  // projections.cpp:676-772: the raw header / view records of a file
+  static bool copyHeader(const char* filename, std::ostream& os);
+  static bool copyViewData(const char* filename, std::ostream& os, int startView, int endView);
+  // projections.cpp:953-995 on the device: polar image of these projections
+  // (interpolateToParallel first for fan beams); interpID from
+  // convertInterpNameToID ("nearest" 0, "bilinear" 1)
+  bool convertPolar(ImageFile& rIF, int iInterpolationID) const;
+  static int convertInterpNameToID(const char* interpName);
   // contiguous storage: row i at rowData() + i * pitch()
   float* rowData() { return m_data.data(); }
   const float* rowData() const { return m_data.data(); }
@@ -204,8 +215,20 @@ class ImageFile {
   bool fileWrite(const char* filename);
   bool fileWrite(const std::string& f) { return fileWrite(f.c_str()); }
   bool fileRead(const char* filename);
+  // imagefile.cpp:186-256 and :378-528 on the device (real FP32 images)
+  bool comparativeStatistics(const ImageFile& imComp, double& d, double& r, double& e) const;
+  bool printComparativeStatistics(const ImageFile& imComp, std::ostream& os) const;
+  bool addImages(const ImageFile& rRHS, ImageFile& result) const;
+  bool subtractImages(const ImageFile& rRHS, ImageFile& result) const;
+  bool multiplyImages(const ImageFile& rRHS, ImageFile& result) const;
+  bool divideImages(const ImageFile& rRHS, ImageFile& result) const;
+  // Array2dFile::labelsCopy (array2dfile.cpp:660-672)
+  void labelsCopy(const ImageFile& copyFile, const char* idPrefix = 0);
+  int getNumLabels() const { return (int)m_labels.size(); }
+  std::string labelText(int i) const { return m_labels[i].text; }
 
  private:
+  bool arith(const char* op, const ImageFile& rRHS, ImageFile& result) const;
   int m_nx, m_ny;
   std::vector<float> m_data;
   std::vector<float*> m_cols;

@@ -188,6 +188,15 @@ def make_io(tmp):
         with open(iff, "rb") as f:
             out[name + "/pj2if_head"] = np.frombuffer(f.read(88), np.uint8)
         out[name + "/pj2if_labels"] = np.array([[l[0], l[1]] for l in im.labels], dtype=object)
+        if name == IO_SCANS[0]:   # pjinfo's four outputs (tools/pjinfo.cpp)
+            for key, extra in (("info", []), ("dump", ["--dump", "--startview", "2",
+                                                         "--endview", "5"]),
+                               ("binhdr", ["--binaryheader"]),
+                               ("binviews", ["--binaryviews", "--startview", "3", "--endview",
+                                             "4"])):
+                r = subprocess.run([REF, "pjinfo", pjf] + extra, check=True,
+                                   capture_output=True)
+                out["pjinfo/" + key] = np.frombuffer(r.stdout, np.uint8)
     # image pairs: rasteriser vs reconstruction, odd sizes, identical, random
     fa, fb = os.path.join(tmp, "a.if"), os.path.join(tmp, "b.if")
     pjs = os.path.join(tmp, "s.pj")
