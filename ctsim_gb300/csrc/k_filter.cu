@@ -67,7 +67,10 @@ cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s) {
   const int N = L.fftN;
   if (N < 4 || (N & (N - 1)) || N > 16384 || N < 2 * L.nDet - 1) return cudaErrorInvalidValue;
   const size_t smem = sizeof(float2) * (size_t)fft_smem_elems(N);
-  int T = N / 8;
+#ifndef CTGPU_FILTER_WIDE
+#define CTGPU_FILTER_WIDE 16   // threads per block = N / CTGPU_FILTER_WIDE (two butterflies each)
+#endif
+  int T = N / CTGPU_FILTER_WIDE;
   if (T < 32) T = 32;
   if (T > 1024) T = 1024;
   const bool one = T * 8 >= N;
