@@ -28,24 +28,29 @@ namespace ctgpu {
 namespace {
 
 struct ElemView {
-  // first 16 bytes, read together by the ray loop: rays t outside [tlo, thi]
-  // cannot reach the outline box's circumcircle (tlo > thi: no ray of this
-  // view meets the element); t_c = tcI + tcF with ftc = (float)tcI
+  // in the order the ray loop reads them, as 16-byte words:
+  // [0] rays t outside [tlo, thi] cannot reach the outline box's circumcircle
+  // (tlo > thi: no ray of this view meets the element); t_c = tcI + tcF with
+  // ftc = (float)tcI
   int tlo, thi;
   float ftc, tcF;
-  float kB;          // rho = kB * (t - t_c)   (times 1/|r| for fan beams)
-  int tcI;
+  // [16] rho = kB * (t - t_c) (times 1/|r| for fan beams); equiangular:
+  // cos/sin of psi'; circumscribed radius of the outline box
+  float kB, cpsi, spsi, rbox;
+  // [32] outline box centre minus element centre, its inscribed radius less
+  // the margin, element type
+  float dcbx, dcby, rin;
   int type;
-  float ca, sa;      // element rotation
-  float u, v, atten;
-  float dcbx, dcby;  // outline box centre minus element centre
-  float hx, hy, rbox;
-  float cpsi, spsi;  // equiangular: cos/sin of psi'
-  float ra, rb;      // parallel: ray direction in the element frame
-  float rin;         // radius of the outline box's inscribed circle, less the margin
-  // E = (ra/u)^2 + (rb/v)^2 of a unit ray direction (rx, ry) as a quadratic
-  // form, E = qa rx^2 + qb rx ry + qc ry^2, and u v (ellipse chords)
+  // [48] E = (ra/u)^2 + (rb/v)^2 of a unit ray direction (rx, ry) as a
+  // quadratic form, E = qa rx^2 + qb rx ry + qc ry^2, and u v (ellipse chords)
   float qa, qb, qc, uv;
+  // [64] outline box half sizes, attenuation
+  float hx, hy, atten;
+  int tcI;
+  // [80] element rotation and half sizes (other element types)
+  float ca, sa, u, v;
+  // [96] parallel: ray direction in the element frame
+  float ra, rb;
   int pad0, pad1;
 };
 static_assert(sizeof(ElemView) % 16 == 0, "ElemView records keep 16-byte alignment");
@@ -137,6 +142,18 @@ __device__ float element_chord(const ElemView& e, float rho, float rx, float ry,
   return hi > lo ? hi - lo : 0.f;
 }
 
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+
+// element_chord's ellipse case from the record's [48] word (qa, qb, qc, uv)
+__device__ __forceinline__ float ellipse_chord(float4 q, float rho, float rx, float ry) {
+  const float E = fmaf(rx * rx, q.x, fmaf(rx * ry, q.y, ry * ry * q.z));
+  const float h = q.w * sqrt_fast(E);
+  const float as = fabsf(rho);
+  if (as >= h) return 0.f;
+  const float hc = sqrt_fast((h - as) * (h + as));
+  return __fdividef(2.f * hc, E * q.w);
+}
+
 // Cohen-Sutherland region code / clip, FP64 (libctsupport/clip.cpp:331-395).
 __device__ int rect_code(double x, double y, const double r[4]) {
   int c = 0;
@@ -166,9 +183,9 @@ __device__ bool clip_rect_fp64(double x1, double y1, double x2, double y2, const
 // +1 clearly hits, -1 clearly misses, 0 within the rounding margin.  The line
 // at distance |rhob| from the box centre meets the box exactly when
 // |rhob| <= hx |ry| + hy |rx| (the box's half-width along the line's normal).
-__device__ __forceinline__ int box_test(const ElemView& e, float rhob, float rx, float ry) {
-  const float m = fmaf(e.hx, fabsf(ry), e.hy * fabsf(rx)) - fabsf(rhob);
-  const float margin = 1e-5f * (e.hx + e.hy) + 1e-9f;
+__device__ __forceinline__ int box_test(float hx, float hy, float rhob, float rx, float ry) {
+  const float m = fmaf(hx, fabsf(ry), hy * fabsf(rx)) - fabsf(rhob);
+  const float margin = 1e-5f * (hx + hy) + 1e-9f;
   if (m > margin) return 1;
   if (m < -margin) return -1;
   return 0;
@@ -436,27 +453,33 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
         if (t < hdr.x || t > hdr.y) continue;
         // integers below 2^24: (float)tcI - ft is the exact (float)(tcI - t)
         const float ftc = __int_as_float(hdr.z), tcF = __int_as_float(hdr.w);
+        const float4 w1 = ld4(&e.kB);     // kB, cpsi, spsi, rbox
         float rho;
         if (GEOM == kEquiangular) {
           float x = ((ftc - ft) + tcF) * hdelta;
-          float cf = fmaf(e.cpsi, cj, e.spsi * sj);
-          rho = e.kB * cf * sin_series(x) * invr;
+          float cf = fmaf(w1.y, cj, w1.z * sj);
+          rho = w1.x * cf * sin_series(x) * invr;
         } else {
           float dt = (ft - ftc) - tcF;
-          rho = e.kB * dt * invr;
+          rho = w1.x * dt * invr;
         }
         // cull against the outline box's circumcircle
-        float rhob = rho + (rx * e.dcby - ry * e.dcbx);
+        const float4 w2 = ld4(&e.dcbx);   // dcbx, dcby, rin, type
+        float rhob = rho + (rx * w2.y - ry * w2.x);
         const float arhob = fabsf(rhob);
-        if (arhob > e.rbox) continue;
-        float ra = 0.f, rb = 0.f;
-        if (e.type != kEllipse) {
+        if (arhob > w1.w) continue;
+        float ch;
+        if (__float_as_int(w2.w) == kEllipse) {
+          ch = ellipse_chord(ld4(&e.qa), rho, rx, ry);
+        } else {
+          float ra, rb;
           if (GEOM == kParallel) { ra = e.ra; rb = e.rb; }
           else { ra = rx * e.ca + ry * e.sa; rb = -rx * e.sa + ry * e.ca; }
+          ch = element_chord(e, rho, rx, ry, ra, rb);
         }
-        float ch = element_chord(e, rho, rx, ry, ra, rb);
         if (ch <= 0.f) continue;
-        int bt = arhob < e.rin ? 1 : box_test(e, rhob, rx, ry);
+        const float4 w4 = ld4(&e.hx);     // hx, hy, atten, tcI
+        int bt = arhob < w2.z ? 1 : box_test(w4.x, w4.y, rhob, rx, ry);
         if (bt == 0) {
           // repeat the reference's FP64 box clip on this ray's end points
           const PElem& pe = elems[k];
@@ -480,7 +503,7 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
           bt = clip_rect_fp64(xd, yd, xs, ys, lim) ? 1 : -1;
         }
         if (bt < 0) continue;
-        sum = fmaf(ch, e.atten, sum);
+        sum = fmaf(ch, w4.z, sum);
       }
     }
     sino[(size_t)(L.rowOffset + view) * L.pitch + d] = sum / fnS;
