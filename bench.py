@@ -650,7 +650,13 @@ def run_gpu(args):
                              "frac": traffic / bp_s / 1e9 / hbm if traffic else None},
                      "gather": {"bytes_per_pixel_view": BYTES_PER_PV,
                                 "achieved_gbs": BYTES_PER_PV * PV_PER_SLICE * B / bp_s / 1e9,
-                                "served_from": "shared memory"}},
+                                "served_from": "shared memory (rows staged by bulk copies)",
+                                "peak_gbs": sms * 128 * sm_mhz * 1e6 / 1e9,
+                                "peak_source": "nominal shared-memory bandwidth, %d SMs x 128 B "
+                                               "per clock x %.0f MHz; no measured figure"
+                                               % (sms, sm_mhz),
+                                "frac": BYTES_PER_PV * PV_PER_SLICE * B / bp_s / 1e9 /
+                                        (sms * 128 * sm_mhz * 1e6 / 1e9)}},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                          "sample": cpu_sample},
         "e2e": {"value": PV_PER_SLICE * B * e2e_steps * world / e2e_s, "unit": UNIT,
