@@ -633,6 +633,16 @@ def run_gpu(args):
                     "ms_per_step": ray_ms / steps,
                     "ray_element_pairs_per_s": RAYS_PER_SLICE * 12 * B * steps * world / (ray_ms / 1e3),
                     "launch": "all %d phantoms in one launch" % B,
+                    # nominal 60 FLOP per ray-element pair (box test, two affine
+                    # maps, circle clip with its square root, back-map and length)
+                    "roofline": {"bound": "fp32 issue", "flop_per_pair": 60,
+                                 "achieved": RAYS_PER_SLICE * 12 * B * steps * world * 60 /
+                                             (ray_ms / 1e3) / 1e12,
+                                 "peak": fp32_peak, "unit": "TFLOP/s",
+                                 "frac": RAYS_PER_SLICE * 12 * B * steps * world * 60 /
+                                         (ray_ms / 1e3) / 1e12 / fp32_peak,
+                                 "note": "set-up and ray kernels together; ncu: issue slots "
+                                         "~82 % busy (profiles/raysum_equiangular_733x720_ncu.md)"},
                     "cpu_baseline": {"value": cpu_raysum_rate[0], "unit": "ray-sums/s",
                                      "cores": cpu_threads, "kind": "port",
                                      "sample": "one 733 x 720 equiangular scan of 12 ellipses"}},
