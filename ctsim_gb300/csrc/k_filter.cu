@@ -23,11 +23,11 @@
 
 namespace ctgpu {
 
-// M = N / (8 blockDim): 1 up to N = 8192, 2 for N = 16384 (a template
-// parameter, so that each kernel holds only the registers its passes use)
-template <int M>
-__global__ void __launch_bounds__(1024) fft_filter_kernel(FilterLaunch L) {
-  extern __shared__ float2 zb[];   // swizzled: element m at zb[fpad(m)]
+// M = N / (8 blockDim) (1 or 2) and the block's thread limit are template
+// parameters, so that each kernel holds only the registers its passes use
+template <int M, int MAXT>
+__global__ void __launch_bounds__(MAXT) fft_filter_kernel(FilterLaunch L) {
+  extern __shared__ float2 zb[];   // swizzled: element m at zb[fpad<M>(m)]
   const int N = L.fftN, n = L.nDet;
   const int v0 = 2 * blockIdx.x;
   const bool two = v0 + 1 < L.nViews;
@@ -41,22 +41,22 @@ __global__ void __launch_bounds__(1024) fft_filter_kernel(FilterLaunch L) {
       v.x = w * ia[m];
       if (two) v.y = w * ib[m];
     }
-    zb[fpad(m)] = v;
+    zb[fpad<M>(m)] = v;
   }
   __syncthreads();
   fft_forward_m<M>(zb, N, L.twiddle);
   // multiply by the kernel's spectrum; conjugate, so that the forward
   // transform below is the inverse one
   for (int m = threadIdx.x; m < N; m += blockDim.x) {
-    const float2 z = cmul(zb[fpad(m)], __ldg(&L.spectrum[m]));
-    zb[fpad(m)] = make_float2(z.x, -z.y);
+    const float2 z = cmul(zb[fpad<M>(m)], __ldg(&L.spectrum[m]));
+    zb[fpad<M>(m)] = make_float2(z.x, -z.y);
   }
   __syncthreads();
   fft_forward_m<M>(zb, N, L.twiddle);
   float* oa = L.out + (size_t)blockIdx.y * L.outSliceStride + (size_t)v0 * L.outPitch;
   float* ob = oa + L.outPitch;
   for (int m = threadIdx.x; m < n; m += blockDim.x) {
-    const float2 y = zb[fpad(m)];
+    const float2 y = zb[fpad<M>(m)];
     oa[m] = y.x;
     if (two) ob[m] = -y.y;
   }
@@ -74,18 +74,21 @@ cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s) {
   if (T < 32) T = 32;
   if (T > 1024) T = 1024;
   const bool one = T * 8 >= N;
+  // the radix-16 passes (M = 2) want about 70 registers: a block limit of 256
+  // threads lets the compiler keep them; larger limits only where needed
+  auto kern = one ? (T > 512 ? fft_filter_kernel<1, 1024>
+                     : T > 256 ? fft_filter_kernel<1, 512> : fft_filter_kernel<1, 256>)
+                  : (T > 512 ? fft_filter_kernel<2, 1024>
+                     : T > 256 ? fft_filter_kernel<2, 512> : fft_filter_kernel<2, 256>);
   if (smem > 48 * 1024) {
-    cudaError_t e = one ? cudaFuncSetAttribute(fft_filter_kernel<1>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                        : cudaFuncSetAttribute(fft_filter_kernel<2>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
   }
   const int nBatch = L.nBatch > 0 ? L.nBatch : 1;
   if (nBatch > 65535) return cudaErrorInvalidConfiguration;
   dim3 grid((L.nViews + 1) / 2, nBatch);
-  if (one) fft_filter_kernel<1><<<grid, T, smem, s>>>(L);
-  else fft_filter_kernel<2><<<grid, T, smem, s>>>(L);
+  kern<<<grid, T, smem, s>>>(L);
   return cudaGetLastError();
 }
 

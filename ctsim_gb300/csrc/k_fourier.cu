@@ -121,17 +121,17 @@ __global__ void __launch_bounds__(256) polar_kernel(PolarLaunch L) {
   if (L.outIm) L.outIm[o] = (float)vi;
 }
 
-// direct DFT of z (swizzled layout, element j at z[fpad(j)]; sign -1 forward,
+// direct DFT of z (swizzled layout, element j at z[fpad_rt(j, sh)]; sign -1 forward,
 // +1 backward) into out[n] (plain layout), shared memory
 __device__ void dft_direct(const float2* z, float2* out, int n, const float2* __restrict__ tw,
-                           int sign) {
+                           int sign, int sh) {
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
     float sr = 0.f, si = 0.f;
     int idx = 0;   // j k mod n, advanced by k
     for (int j = 0; j < n; j++) {
       const float2 w = __ldg(&tw[idx]);
       const float wi = sign < 0 ? w.y : -w.y;
-      const float2 zj = z[fpad(j)];
+      const float2 zj = z[fpad_rt(j, sh)];
       sr = fmaf(zj.x, w.x, fmaf(-zj.y, wi, sr));
       si = fmaf(zj.x, wi, fmaf(zj.y, w.x, si));
       idx += k;
@@ -144,21 +144,21 @@ __device__ void dft_direct(const float2* z, float2* out, int n, const float2* __
 // transform buf (swizzled layout) in place (pow2: Stockham; else direct DFT
 // through tmp)
 __device__ __forceinline__ void line_transform(float2* buf, float2* tmp, int n,
-                                               const float2* __restrict__ tw, int sign) {
+                                               const float2* __restrict__ tw, int sign, int sh) {
   if ((n & (n - 1)) == 0) {
     if (sign > 0)   // backward = conj(forward(conj))
-      for (int m = threadIdx.x; m < n; m += blockDim.x) buf[fpad(m)].y = -buf[fpad(m)].y;
+      for (int m = threadIdx.x; m < n; m += blockDim.x) buf[fpad_rt(m, sh)].y = -buf[fpad_rt(m, sh)].y;
     __syncthreads();
     if (n > 1) fft_forward(buf, n, tw);
     if (sign > 0) {
-      for (int m = threadIdx.x; m < n; m += blockDim.x) buf[fpad(m)].y = -buf[fpad(m)].y;
+      for (int m = threadIdx.x; m < n; m += blockDim.x) buf[fpad_rt(m, sh)].y = -buf[fpad_rt(m, sh)].y;
       __syncthreads();
     }
   } else {
     __syncthreads();
-    dft_direct(buf, tmp, n, tw, sign);
+    dft_direct(buf, tmp, n, tw, sign, sh);
     __syncthreads();
-    for (int m = threadIdx.x; m < n; m += blockDim.x) buf[fpad(m)] = tmp[m];
+    for (int m = threadIdx.x; m < n; m += blockDim.x) buf[fpad_rt(m, sh)] = tmp[m];
     __syncthreads();
   }
 }
@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(1024) fourier_views_kernel(FourierViewsLaunch 
   float2* buf = zs;                          // swizzled layout
   float2* tmp = zs + fft_smem_elems(L.N);    // direct DFT only
   const int v = blockIdx.x, N = L.N, nI = L.nInterp, nDet = L.nDet;
+  const int sh = fft_swizzle_shift(N);
   const float* row = L.sino + (size_t)v * L.pitch;
   const int zeros = N - nI;
   for (int m = threadIdx.x; m < N; m += blockDim.x) {
@@ -194,14 +195,14 @@ __global__ void __launch_bounds__(1024) fourier_views_kernel(FourierViewsLaunch 
       }
       val.x = (float)(r * L.projScale);
     }
-    buf[fpad(m)] = val;
+    buf[fpad_rt(m, sh)] = val;
   }
   __syncthreads();
-  line_transform(buf, tmp, N, L.twiddle, -1);
+  line_transform(buf, tmp, N, L.twiddle, -1, sh);
   float2* out = L.spec + (size_t)v * N;
   const float sc = (float)L.fftScale;
   for (int d = threadIdx.x; d < N; d += blockDim.x) {
-    const float2 z = buf[fpad(nat_src(N, d))];
+    const float2 z = buf[fpad_rt(nat_src(N, d), sh)];
     out[d] = make_float2(z.x * sc, z.y * sc);
   }
 }
@@ -216,23 +217,24 @@ __global__ void __launch_bounds__(1024) ifft_lines_kernel(IfftLaunch L, int pass
   float2* buf = zs;                      // swizzled layout
   float2* tmp = zs + fft_smem_elems(n);   // direct DFT only
   const int line = blockIdx.x;
+  const int sh = fft_swizzle_shift(n);
   if (pass == 1) {
     const int sx = fou_src(nx, line);
     for (int m = threadIdx.x; m < ny; m += blockDim.x) {
       const size_t s = (size_t)sx * ny + fou_src(ny, m);
-      buf[fpad(m)] = make_float2(L.inRe[s], L.inIm[s]);
+      buf[fpad_rt(m, sh)] = make_float2(L.inRe[s], L.inIm[s]);
     }
   } else {
     const int k2 = nat_src(ny, line);   // this CTA writes output row `line`
-    for (int m = threadIdx.x; m < nx; m += blockDim.x) buf[fpad(m)] = L.tmp[(size_t)m * ny + k2];
+    for (int m = threadIdx.x; m < nx; m += blockDim.x) buf[fpad_rt(m, sh)] = L.tmp[(size_t)m * ny + k2];
   }
   __syncthreads();
-  line_transform(buf, tmp, n, pass == 1 ? L.twY : L.twX, +1);
+  line_transform(buf, tmp, n, pass == 1 ? L.twY : L.twX, +1, sh);
   if (pass == 1) {
-    for (int m = threadIdx.x; m < ny; m += blockDim.x) L.tmp[(size_t)line * ny + m] = buf[fpad(m)];
+    for (int m = threadIdx.x; m < ny; m += blockDim.x) L.tmp[(size_t)line * ny + m] = buf[fpad_rt(m, sh)];
   } else {
     for (int d1 = threadIdx.x; d1 < nx; d1 += blockDim.x) {
-      const float2 z = buf[fpad(nat_src(nx, d1))];   // the reference keeps FP32 re / im
+      const float2 z = buf[fpad_rt(nat_src(nx, d1), sh)];   // the reference keeps FP32 re / im
       const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(z.x, z.x), __fmul_rn(z.y, z.y)));
       L.out[(size_t)d1 * ny + line] = mag;
     }
