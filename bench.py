@@ -494,16 +494,6 @@ def fourier_recon(args, torch, cg, device, sinos, g, angles, B):
                              "(radix-2 FFTs)"}}
 
 
-def chunks(b):
-    """slice chunks of ctgpu_recon_run_batch_host: 8, 24, then 32"""
-    out, nxt = [], 8
-    while b > 0:
-        out.append(min(nxt, b))
-        b -= out[-1]
-        nxt = 24 if nxt == 8 else 32
-    return out
-
-
 def run_gpu(args):
     import torch
     import ctsim_gb300 as cg
@@ -588,6 +578,7 @@ def run_gpu(args):
     # host memory
     host_sinos = sinos[:, :, :N_DET].contiguous().cpu().pin_memory()
     host_images = torch.zeros((B, NX, NX), dtype=torch.float32).pin_memory()
+    e2e_chunks = plan.host_chunks(B)
     plan.run_batch_host(host_sinos, angles[0], host_images)
     barrier(world)
     e2e_steps = max(1, args.steps)
@@ -670,11 +661,11 @@ def run_gpu(args):
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                          "sample": cpu_sample},
         "e2e": {"value": PV_PER_SLICE * B * e2e_steps * world / e2e_s, "unit": UNIT,
-                "h2d_bytes_per_step": B * N_VIEW * N_DET * 4 + len(chunks(B)) * N_VIEW * 8,
+                "h2d_bytes_per_step": B * N_VIEW * N_DET * 4 + len(e2e_chunks) * N_VIEW * 8,
                 "d2h_bytes_per_step": B * NX * NX * 4,
                 "steps": e2e_steps, "ms_per_step": e2e_s / e2e_steps * 1e3,
                 "path": "ctgpu_recon_run_batch_host (page-locked host buffers, chunks of "
-                        "%s slices, copies overlapped with compute)" % "+".join(map(str, chunks(B))),
+                        "%s slices, copies overlapped with compute)" % "+".join(map(str, e2e_chunks)),
                 "parity_vs_device_rel_l2": e2e_err,
                 "single_slice_run_host_rel_l2": single_err},
         # per step: one filter launch; interval rows, tile records and the

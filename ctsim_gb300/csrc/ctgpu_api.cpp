@@ -1051,11 +1051,16 @@ static BackprojLaunch make_launch(const ctgpu_recon* r, int nViews, int pitch,
 }
 
 // Backprojection of nViews filtered rows; outScale multiplies this launch's sum.
+// reuseScratch: the scratch whose (tile, view) records an earlier launch on
+// stream st built for the same view angles (table family), or null;
+// anglesOnDevice: r->d_angles already holds h_angles, ordered before st's work
 static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int pitch,
                                     const double* h_angles, int nViews, float* d_image,
                                     int accumulate, float outScale, cudaStream_t st,
                                     int nBatch = 1, size_t filtStride = 0,
-                                    size_t imageStride = 0) {
+                                    size_t imageStride = 0,
+                                    const unsigned char* reuseScratch = nullptr,
+                                    bool anglesOnDevice = false) {
   if (nViews <= 0) {
     if (!accumulate)
       for (int b = 0; b < nBatch; b++)
@@ -1070,8 +1075,10 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
     }
     return ok();
   }
-  CUDA_TRY(ensure_device(r->d_angles, r->d_angles_cap, (size_t)nViews));
-  CUDA_TRY(cudaMemcpyAsync(r->d_angles, h_angles, sizeof(double) * nViews, cudaMemcpyHostToDevice, st));
+  if (!anglesOnDevice) {
+    CUDA_TRY(ensure_device(r->d_angles, r->d_angles_cap, (size_t)nViews));
+    CUDA_TRY(cudaMemcpyAsync(r->d_angles, h_angles, sizeof(double) * nViews, cudaMemcpyHostToDevice, st));
+  }
   const void* views = nullptr;
   if (r->bproj == kIDiff || r->bproj == kDiff) {
     // per-view steps in the reference's own FP64 / fixed-point arithmetic
@@ -1100,7 +1107,11 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
   BackprojLaunch L = make_launch(r, nViews, pitch, r->d_angles, d_filtered, d_image, accumulate,
                                  outScale, nBatch, filtStride, imageStride);
   size_t sb = backproject_scratch_bytes(L);
+  const size_t capBefore = r->d_scratch_cap;
   if (sb) CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
+  // a reallocated scratch (even at the same address) holds no records
+  L.reuseRecords = reuseScratch && reuseScratch == r->d_scratch && r->d_scratch_cap == capBefore &&
+                   r->bproj != kDiff && r->bproj != kIDiff;
   cudaError_t e = launch_backproject_views(L, views, r->d_scratch, st);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "image pixels behind the fan-beam source");
@@ -1168,9 +1179,22 @@ int ctgpu_recon_run_host(ctgpu_recon* r, const float* h_sino, const double* h_an
   return ctgpu_sync(nullptr);
 }
 
+static int recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int sinoPitch,
+                           long long sinoSliceStride, const double* h_angles, float* d_images,
+                           long long imageSliceStride, int flags, cudaStream_t st,
+                           const unsigned char* reuseScratch, bool anglesOnDevice);
+
 int ctgpu_recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int sinoPitch,
                           long long sinoSliceStride, const double* h_angles, float* d_images,
                           long long imageSliceStride, int flags, void* stream) {
+  return recon_run_batch(r, nBatch, d_sinos, sinoPitch, sinoSliceStride, h_angles, d_images,
+                         imageSliceStride, flags, (cudaStream_t)stream, nullptr, false);
+}
+
+static int recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int sinoPitch,
+                           long long sinoSliceStride, const double* h_angles, float* d_images,
+                           long long imageSliceStride, int flags, cudaStream_t st,
+                           const unsigned char* reuseScratch, bool anglesOnDevice) {
   if (!r || !d_sinos || !h_angles || !d_images) return fail(CTGPU_ERR_INVALID, "null argument");
   if (nBatch < 1) return fail(CTGPU_ERR_INVALID, "batch size must be >= 1");
   const int nView = r->g.n_view;
@@ -1178,7 +1202,6 @@ int ctgpu_recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int 
       imageSliceStride < (long long)r->nx * r->ny)
     return fail(CTGPU_ERR_INVALID, "pitch / slice strides too small");
   if (flags & CTGPU_RUN_ACCUMULATE) return fail(CTGPU_ERR_UNSUPPORTED, "batched runs overwrite their images");
-  cudaStream_t st = (cudaStream_t)stream;
   size_t fStride = (size_t)nView * r->pitch;
   CUDA_TRY(ensure_device(r->d_filtered, r->d_filtered_cap, fStride * nBatch));
   int rc = recon_filter_batch(r, d_sinos, sinoPitch, (size_t)sinoSliceStride, nView,
@@ -1188,7 +1211,70 @@ int ctgpu_recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int 
   bool post = (flags & CTGPU_RUN_POSTPROCESS) != 0;
   if (post && r->bproj != kTrig) scale = (float)(scale * r->rotScale);
   return recon_backproject_scaled(r, r->d_filtered, r->pitch, h_angles, nView, d_images, 0, scale,
-                                  st, nBatch, fStride, (size_t)imageSliceStride);
+                                  st, nBatch, fStride, (size_t)imageSliceStride, reuseScratch,
+                                  anglesOnDevice);
+}
+
+// Chunk sizes of a host-buffer batch.  A backprojection launch of s slices
+// runs ceil(s * tiles / resident) waves of blocks: a wave is paid whole
+// however few of its blocks have work.  The first chunk's input copy and the
+// last chunk's output copy are not hidden behind compute; every other copy
+// is.  The sizes minimise, by dynamic programming over the slices, the waves
+// plus the two exposed copies plus a fixed cost per chunk, all in
+// milliseconds from rough GB300 rates (1.1e12 pixel-view updates/s, 200 GB/s
+// host to device, 180 GB/s back, 20 us between chunks).
+static std::vector<int> plan_chunks(int nBatch, int maxChunk, long long tilesPerSlice,
+                                    long long resident, double waveMs, double inMs, double outMs) {
+  const double chunkMs = 0.02;
+  auto body = [&](int sz) {
+    const long long ctas = tilesPerSlice * sz;
+    return (double)((ctas + resident - 1) / resident) * waveMs + chunkMs;
+  };
+  const double inf = 1e300;
+  std::vector<double> best(nBatch + 1, inf);
+  std::vector<int> last(nBatch + 1, 0);
+  best[0] = 0;
+  for (int i = 1; i <= nBatch; i++)
+    for (int sz = 1; sz <= maxChunk && sz <= i; sz++) {
+      double c = best[i - sz] + body(sz) + (i == sz ? inMs * sz : 0.0) + (i == nBatch ? outMs * sz : 0.0);
+      if (c < best[i]) {
+        best[i] = c;
+        last[i] = sz;
+      }
+    }
+  std::vector<int> sizes;
+  for (int i = nBatch; i > 0; i -= last[i]) sizes.push_back(last[i]);
+  std::reverse(sizes.begin(), sizes.end());
+  return sizes;
+}
+
+// the chunks of a host-buffer batch of nBatch slices on the current device
+static cudaError_t host_chunk_sizes(const ctgpu_recon* r, int nBatch, std::vector<int>* sizes) {
+  const int nView = r->g.n_view;
+  const size_t sStride = (size_t)nView * r->g.n_det, iStride = (size_t)r->nx * r->ny;
+  int sms = 0, dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  // at most 64 slices and 1 GiB of staging per chunk buffer
+  const size_t sliceBytes = sizeof(float) * (sStride + iStride);
+  const int maxChunk = (int)std::max<size_t>(1, std::min<size_t>(64, (1ull << 30) / sliceBytes));
+  const long long tilesPerSlice = (long long)((r->nx + kBackprojTile - 1) / kBackprojTile) *
+                                  ((r->ny + kBackprojTile - 1) / kBackprojTile);
+  const long long resident = (long long)sms * backproject_table_ctas_per_sm();
+  const double waveMs = (double)resident * kBackprojTile * kBackprojTile * nView / 1.1e9;
+  *sizes = plan_chunks(nBatch, maxChunk, tilesPerSlice, resident, waveMs,
+                       sizeof(float) * sStride / 2e8, sizeof(float) * iStride / 1.8e8);
+  return cudaSuccess;
+}
+
+int ctgpu_recon_host_chunks(const ctgpu_recon* r, int nBatch, int* sizes, int maxSizes) {
+  if (!r || (!sizes && maxSizes > 0)) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (nBatch < 1) return fail(CTGPU_ERR_INVALID, "batch size must be >= 1");
+  std::vector<int> v;
+  CUDA_TRY(host_chunk_sizes(r, nBatch, &v));
+  for (int i = 0; i < (int)v.size() && i < maxSizes; i++) sizes[i] = v[i];
+  return (int)v.size();
 }
 
 int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
@@ -1197,19 +1283,17 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
   if (nBatch < 1) return fail(CTGPU_ERR_INVALID, "batch size must be >= 1");
   if (flags & CTGPU_RUN_ACCUMULATE) return fail(CTGPU_ERR_UNSUPPORTED, "batched runs overwrite their images");
   const int nDet = r->g.n_det, nView = r->g.n_view;
-  // chunks of 8, 24, then 32 slices: a small first chunk starts the
-  // reconstruction early, larger ones keep the backprojection launches full
-  std::vector<int> sizes, first;
-  for (int left = nBatch, next = 8; left > 0; next = next == 8 ? 24 : 32) {
-    const int n = left < next ? left : next;
-    first.push_back(nBatch - left);
-    sizes.push_back(n);
-    left -= n;
-  }
-  const int chunk = nBatch < 32 ? nBatch : 32;
   // input rows arrive dense ([slice][view][n_det], one plain copy per chunk);
   // the filter reads them at pitch n_det and writes the aligned filtered rows
   const size_t sStride = (size_t)nView * nDet, iStride = (size_t)r->nx * r->ny;
+  std::vector<int> sizes;
+  CUDA_TRY(host_chunk_sizes(r, nBatch, &sizes));
+  std::vector<int> first;
+  int chunk = 0;
+  for (size_t c = 0, at = 0; c < sizes.size(); at += sizes[c], c++) {
+    first.push_back((int)at);
+    chunk = std::max(chunk, sizes[c]);
+  }
   CUDA_TRY(ensure_device(r->d_bsino, r->d_bsino_cap, 2 * chunk * sStride));
   CUDA_TRY(ensure_device(r->d_bimage, r->d_bimage_cap, 2 * chunk * iStride));
   if (r->h_angles_cap < (size_t)nView) {
@@ -1224,14 +1308,29 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
     if (!*s) CUDA_TRY(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking));
   for (cudaEvent_t& e : r->ev)
     if (!e) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  // the per-chunk angle uploads then come from page-locked memory and never
-  // wait for the compute stream on the host (the last call's copies are done:
-  // each call ends synchronised)
+  // the angles go up once, from page-locked memory, on the input stream ahead
+  // of the first chunk (the last call's copies are done: each call ends
+  // synchronised).  Uploaded per chunk on the compute stream, a chunk's
+  // angles queued behind the next chunk's input copy in the same direction.
   std::memcpy(r->h_angles_pinned, h_angles, sizeof(double) * nView);
+  CUDA_TRY(ensure_device(r->d_angles, r->d_angles_cap, (size_t)nView));
+  CUDA_TRY(cudaMemcpyAsync(r->d_angles, r->h_angles_pinned, sizeof(double) * nView,
+                           cudaMemcpyHostToDevice, r->s_in));
   cudaEvent_t* inDone = r->ev;
   cudaEvent_t* compDone = r->ev + 2;
   cudaEvent_t* outDone = r->ev + 4;
   const int nChunks = (int)sizes.size();
+  const unsigned char* recScratch = nullptr;
+  {
+    // filtered rows and scratch for the largest chunk up front: no buffer is
+    // reallocated (a synchronising free) between chunks, and the records stay put
+    const size_t fStride = (size_t)nView * r->pitch;
+    CUDA_TRY(ensure_device(r->d_filtered, r->d_filtered_cap, fStride * chunk));
+    BackprojLaunch L = make_launch(r, nView, r->pitch, nullptr, nullptr, nullptr, 0, 1.f, chunk,
+                                   fStride, iStride);
+    const size_t sb = backproject_scratch_bytes(L);
+    if (sb) CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
+  }
   // image copy of chunk c, issued one iteration late so that a pageable
   // destination (whose copy blocks the host) does not hold back the next
   // chunk's input copy and launch
@@ -1253,9 +1352,13 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
     CUDA_TRY(cudaEventRecord(inDone[b], r->s_in));
     CUDA_TRY(cudaStreamWaitEvent(r->s_comp, inDone[b], 0));
     if (c >= 2) CUDA_TRY(cudaStreamWaitEvent(r->s_comp, outDone[b], 0));   // image b copied out
-    int rc = ctgpu_recon_run_batch(r, n, dS, nDet, (long long)sStride, r->h_angles_pinned, dI,
-                                   (long long)iStride, flags & CTGPU_RUN_POSTPROCESS, r->s_comp);
+    // every chunk has the same view angles: the first builds the (tile, view)
+    // records, the later ones on the same stream use them
+    int rc = recon_run_batch(r, n, dS, nDet, (long long)sStride, r->h_angles_pinned, dI,
+                             (long long)iStride, flags & CTGPU_RUN_POSTPROCESS, r->s_comp,
+                             c > 0 ? recScratch : nullptr, true);
     if (rc) return rc;
+    if (c == 0) recScratch = r->d_scratch;
     CUDA_TRY(cudaEventRecord(compDone[b], r->s_comp));
     if (c >= 1 && (rc = copy_out(c - 1))) return rc;
   }

@@ -99,6 +99,9 @@ struct BackprojLaunch {
   int accumulate;         // add into image instead of overwriting
   float outScale;         // applied to this launch's contribution (rotScale for trig)
   unsigned int* status;
+  // table family: the (tile, view) records in scratch were built by an earlier
+  // launch of the same plan and view angles, ordered before this one
+  int reuseRecords;
 };
 
 struct HelicalLaunch {
@@ -201,6 +204,9 @@ cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int 
                               cudaStream_t s);
 cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
 size_t backproject_scratch_bytes(const BackprojLaunch& L);
+// blocks of the table-family main kernel resident per SM (its occupancy target)
+int backproject_table_ctas_per_sm();
+constexpr int kBackprojTile = 32;   // image pixels per tile side
 
 // The table-family backprojection as set-up launches plus a main launch, for
 // the batched path (many problems of different sizes, one persistent launch).

@@ -180,6 +180,17 @@ class ReconPlan:
                                                RUN_POSTPROCESS if postprocess else 0))
         return out
 
+    def host_chunks(self, n_batch):
+        """the chunk sizes run_batch_host uses for n_batch slices on this GPU"""
+        sizes = (C.c_int * 64)()
+        n = lib().ctgpu_recon_host_chunks(self._h, int(n_batch), C.cast(sizes, C.c_void_p), 64)
+        if n < 0:
+            check(n)
+        if n > 64:
+            sizes = (C.c_int * n)()
+            n = lib().ctgpu_recon_host_chunks(self._h, int(n_batch), C.cast(sizes, C.c_void_p), n)
+        return list(sizes[:n])
+
     def project(self, image, angles, out, scale=1.0, stream=None):
         ang = np.ascontiguousarray(angles, np.float64)
         check(lib().ctgpu_recon_project(self._h, _ptr(image), ang.ctypes.data_as(C.c_void_p),

@@ -214,13 +214,20 @@ int ctgpu_recon_run_batch(ctgpu_recon* r, int n_batch, const float* d_sinos, int
                           void* stream);
 /* ctgpu_recon_run_batch with host buffers: h_sinos n_batch sinograms
  * [n_view][n_det] back to back, h_images n_batch images [nx][ny] back to back.
- * Slices move in chunks of 8, 24, then 32 through two device buffers, so the
- * copy of one chunk overlaps the reconstruction of the previous one (page-locked
- * host buffers make the copies asynchronous; pageable ones work, with less
- * overlap).  Synchronous: returns when h_images is written.  No reference
- * counterpart (CTSim reconstructs one slice per Reconstructor). */
+ * Slices move in chunks through two device buffers, so the copy of one chunk
+ * overlaps the reconstruction of the previous one (page-locked host buffers
+ * make the copies asynchronous; pageable ones work, with less overlap).  The
+ * chunk sizes (ctgpu_recon_host_chunks) keep each backprojection launch to
+ * whole waves of blocks on this GPU and the first and last chunks' copies
+ * short; the chunks share one set of (tile, view) records.  Synchronous:
+ * returns when h_images is written.  No reference counterpart (CTSim
+ * reconstructs one slice per Reconstructor). */
 int ctgpu_recon_run_batch_host(ctgpu_recon* r, int n_batch, const float* h_sinos,
                                const double* h_view_angles, float* h_images, int flags);
+/* The chunk sizes ctgpu_recon_run_batch_host uses for n_batch slices on the
+ * current device: the first min(count, max_sizes) go to sizes; returns the
+ * number of chunks (>= 1), or a negative error.  No reference counterpart. */
+int ctgpu_recon_host_chunks(const ctgpu_recon* r, int n_batch, int* sizes, int max_sizes);
 /* Backprojection of n_batch filtered sinograms (same geometry and angles) in
  * one launch; flags: CTGPU_RUN_POSTPROCESS folds PostProcessing in. */
 int ctgpu_recon_backproject_batch(ctgpu_recon* r, int n_batch, const float* d_filtered,

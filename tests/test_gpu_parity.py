@@ -260,8 +260,8 @@ def test_batched_launch_equals_single(gpu, geo, interp, bp):
 
 @pytest.mark.parametrize("pinned", [False, True])
 def test_batch_host_equals_device_batch(gpu, pinned):
-    """ctgpu_recon_run_batch_host (chunks of 16, copies overlapped) gives the
-    device batch's images; 37 slices = two full chunks and a ragged one."""
+    """ctgpu_recon_run_batch_host (copies overlapped with the reconstruction)
+    gives the device batch's images; 37 slices of 64 x 64."""
     torch, cg, device = gpu
     from ctsim_gb300 import phantoms
     B, nd, nv, n = 37, 129, 90, 64
@@ -290,6 +290,39 @@ def test_batch_host_equals_device_batch(gpu, pinned):
     r = ref.cpu().numpy()
     for b in range(B):
         assert rel_l2(res[b], r[b]) < 1e-7, b
+
+
+def test_batch_host_chunks_share_records(gpu):
+    """A host batch split into chunks of different sizes, a later one larger
+    than the first (buffers sized for the largest up front, the first chunk's
+    (tile, view) records used by the rest): the device batch's images, bit
+    for bit.  The chunk plan covers every slice once for any batch size."""
+    torch, cg, device = gpu
+    from ctsim_gb300 import phantoms
+    nd, nv, n = 367, 360, 256
+    ph0 = phantoms.make_phantom(phantoms.random_ellipses(seed=900, n=5))
+    sc = cg.Scanner(ph0, "equiangular", nd, nv)
+    g = sc.geometry()
+    plan = device.ReconPlan(g, n, n, "abs_hamming", 0.54, "fft", 2, "direct", "cubic", 1, "table")
+    for b in (1, 2, 7, 33, 100, 500):
+        sizes = plan.host_chunks(b)
+        assert sum(sizes) == b and min(sizes) >= 1, (b, sizes)
+    B = next((b for b in (24, 16, 40, 64)
+              if len(plan.host_chunks(b)) >= 2 and max(plan.host_chunks(b)[1:]) > plan.host_chunks(b)[0]),
+             None)
+    assert B is not None, [plan.host_chunks(b) for b in (24, 16, 40, 64)]
+    phs = [phantoms.make_phantom(phantoms.random_ellipses(seed=900 + b, n=5)) for b in range(B)]
+    batch = torch.zeros((B, nv, device.pitch_for(nd)), device="cuda")
+    angs = device.raysums_batch(sc, phs, batch)
+    ref = torch.zeros((B, n, n), device="cuda")
+    plan.run_batch(batch, angs, ref)
+    cg.sync()
+    host = batch[:, :, :nd].contiguous().cpu().pin_memory()
+    out = torch.zeros((B, n, n), dtype=torch.float32).pin_memory()
+    for _ in range(2):   # the second call finds every buffer in place
+        out.zero_()
+        plan.run_batch_host(host, angs, out)
+        assert torch.equal(out, ref.cpu()), plan.host_chunks(B)
 
 
 @pytest.mark.parametrize("geo,nray", [("parallel", 2), ("equiangular", 1), ("equilinear", 3)])
