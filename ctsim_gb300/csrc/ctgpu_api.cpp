@@ -174,6 +174,7 @@ PElem make_elem(int type, double cx, double cy, double u, double v, double rotDe
   // a line this close to the box centre crosses the box for certain: the
   // kernel's FP32 box test margin (1e-5 (hx + hy)) and its rounding stay inside
   e.rin = (float)(std::fmin(hx, hy) - 2e-5 * (hx + hy) - 1e-7);
+  set_elem_quadratic(e);
   return e;
 }
 
@@ -254,9 +255,17 @@ struct ctgpu_scanner {
   size_t d_velems_cap = 0;
   double2* d_zc = nullptr;
   size_t d_zc_cap = 0;
+  // equiangular: (cos, sin) of t * delta for every ray index t (the same for
+  // every view), for the rays' FP64 box decisions; built for arcN rays of
+  // step arcDelta
+  double2* d_arc = nullptr;
+  size_t d_arc_cap = 0;
+  int arcN = 0;
+  double arcDelta = 0;
   ~ctgpu_scanner() {
     for (void* p : {(void*)d_views, (void*)d_sino, (void*)d_belems, (void*)d_boffs,
-                    (void*)d_sdirs, (void*)d_records, (void*)d_velems, (void*)d_zc})
+                    (void*)d_sdirs, (void*)d_records, (void*)d_velems, (void*)d_zc,
+                    (void*)d_arc})
       if (p) cudaFree(p);
   }
 };
@@ -581,6 +590,10 @@ RayView ctgpu::make_ray_view(int geometry, int nDet, int nS, double angularDetLe
   g.sa0 = (float)g.s0;
   g.Sx = (float)g.S0x;
   g.Sy = (float)g.S0y;
+  g.cmf = (float)g.cm;
+  g.smf = (float)g.sm;
+  g.midRelf = (float)g.midRel;
+  g.invDeltaf = (float)g.invDelta;
   return g;
 }
 
@@ -593,7 +606,22 @@ static cudaError_t upload_ray_views(ctgpu_scanner* s, int nViews, cudaStream_t s
   cudaError_t e = ensure_device(s->d_views, s->d_views_cap, (size_t)nViews);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(s->d_views, rv.data(), sizeof(RayView) * nViews, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess || s->geometry != kParallel) return e;
+  if (e != cudaSuccess) return e;
+  if (s->geometry == kEquiangular) {
+    const int n = s->nDet * s->nSample;
+    const double delta = s->angularDetInc / s->nSample;
+    if (s->arcN != n || s->arcDelta != delta) {
+      std::vector<double2> arc(n);
+      for (int t = 0; t < n; t++) arc[t] = make_double2(std::cos(t * delta), std::sin(t * delta));
+      e = ensure_device(s->d_arc, s->d_arc_cap, (size_t)n);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(s->d_arc, arc.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return e;
+      s->arcN = n;
+      s->arcDelta = delta;
+    }
+  }
+  if (s->geometry != kParallel) return e;
   std::vector<float2> dirs((size_t)nViews * s->nSample);
   for (int v = 0; v < nViews; v++)
     for (int i = 0; i < s->nSample; i++) {
@@ -642,6 +670,7 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
   L.elems = p->d_elems;
   L.views = s->d_views;
   L.sdirs = s->d_sdirs;
+  L.arc = s->d_arc;
   L.sino = d_sino;
   L.status = status_pointer();
   CUDA_TRY(ensure_device(s->d_records, s->d_records_cap, raysum_record_bytes(L, L.nElem)));
@@ -696,6 +725,7 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   L.elems = s->d_belems;
   L.views = s->d_views;
   L.sdirs = s->d_sdirs;
+  L.arc = s->d_arc;
   L.sino = d_sinos;
   L.status = status_pointer();
   L.nSlices = n;
@@ -756,6 +786,7 @@ int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ell, in
   L.elems = s->d_velems;
   L.views = s->d_views;
   L.sdirs = s->d_sdirs;
+  L.arc = s->d_arc;
   L.sino = d_sino;
   L.status = status_pointer();
   L.elemsPerView = 1;
@@ -795,6 +826,7 @@ int ctgpu_raysum_ellipse_gradient(ctgpu_scanner* s, const ctgpu_phantom* p,
   L.elems = p->d_elems;
   L.views = s->d_views;
   L.sdirs = s->d_sdirs;
+  L.arc = s->d_arc;
   std::vector<double> g(6 * (size_t)(n > 0 ? n : 1), 0.0);
   cudaError_t e = cudaMemsetAsync(d_grad, 0, sizeof(double) * g.size(), st);
   if (e == cudaSuccess) e = launch_raysum_ellipse_grad(L, d_gsino, d_grad, st);

@@ -28,7 +28,22 @@ struct PElem {
   // box centre minus element centre, box half sizes, circumscribed radius
   // (widened by its margin), inscribed radius less the margin
   float dcbx, dcby, hx, hy, rbox, rin;
+  // ellipse chords: E = (ra/u)^2 + (rb/v)^2 of a unit direction (rx, ry) as
+  // the quadratic form qa rx^2 + qb rx ry + qc ry^2, and u v (FP32 products
+  // of the FP32 semi-axes); set by set_elem_quadratic
+  float qa, qb, qc, uv;
 };
+
+// PElem's ellipse quadratic form from its semi-axes and rotation (FP64, then
+// FP32): once per element, not per view
+__host__ __device__ inline void set_elem_quadratic(PElem& e) {
+  const double iu2 = 1.0 / (e.u * e.u), iv2 = 1.0 / (e.v * e.v);
+  const double c = e.cosr, sn = e.sinr;
+  e.qa = (float)(c * c * iu2 + sn * sn * iv2);
+  e.qb = (float)(2.0 * c * sn * (iu2 - iv2));
+  e.qc = (float)(sn * sn * iu2 + c * c * iv2);
+  e.uv = (float)e.u * (float)e.v;
+}
 
 // Source / detector end points of one view after the reference's incremental
 // rotation (libctsim/scanner.cpp:301-417), and its view angle.
@@ -46,7 +61,7 @@ struct RayView {
   double midRel, invDelta;         // middle - alpha0, 1 / delta
   float rsx, rsy, stx, sty;        // FP32: D0 - S0, per-ray step
   float hdelta, ca0, sa0, Sx, Sy;  // FP32: delta / 2, cos/sin alpha0, source
-  float pad[3];
+  float cmf, smf, midRelf, invDeltaf;   // FP32: cm, sm, midRel, invDelta
 };
 RayView make_ray_view(int geometry, int nDet, int nSample, double angularDetLen,
                       double angularDetInc, const ViewPos& vp);
@@ -57,6 +72,7 @@ struct RaysumLaunch {
   const PElem* elems;
   const RayView* views;   // nViews
   const float2* sdirs;    // parallel: [nViews][nSample] unit ray directions
+  const double2* arc;     // equiangular: (cos, sin) of t * delta, t < nDet * nSample
   void* records;          // scratch: raysum_record_bytes()
   float* sino;
   unsigned int* status;
@@ -69,6 +85,10 @@ struct RaysumLaunch {
   // one element list per view (3-D phantoms): view v's nElem elements start
   // at elems + v * nElem; an element of type < 0 is absent from that view
   int elemsPerView;
+  // set by launch_raysum: 1 / centerDetectorLength, and atan(j / 64) for
+  // j = 0..64 (the record set-up's table-driven arctangent)
+  double invCD;
+  double atan64[65];
 };
 
 // Filter: out[v][n] = sum_i (w[i] * in[v][i]) * taps[n - i + nDet - 1]

@@ -18,9 +18,14 @@
 // equiangular arc the numerator is a difference of sines, rewritten as
 // 2 cos(.) sin((alpha_c - alpha_t)/2) with a small, accurately formed argument.
 // The pre-rejection box is tested in FP32 with a margin; rays within the
-// margin of the box boundary repeat the reference's FP64 Cohen-Sutherland test.
+// margin of the box boundary are decided in FP64 on their end points (the
+// line-box test that the reference's Cohen-Sutherland clip amounts to here).
 //
 // One CTA per view: the per-view FP64 setup is paid once per view.
+#include <algorithm>
+#include <array>
+#include <cmath>
+
 #include "ctgpu_internal.h"
 
 namespace ctgpu {
@@ -154,29 +159,19 @@ __device__ __forceinline__ float ellipse_chord(float4 q, float rho, float rx, fl
   return __fdividef(2.f * hc, E * q.w);
 }
 
-// Cohen-Sutherland region code / clip, FP64 (libctsupport/clip.cpp:331-395).
-__device__ int rect_code(double x, double y, const double r[4]) {
-  int c = 0;
-  if (x < r[0]) c = 1;
-  else if (x > r[2]) c = 2;
-  if (y < r[1]) c += 4;
-  else if (y > r[3]) c += 8;
-  return c;
-}
-__device__ bool clip_rect_fp64(double x1, double y1, double x2, double y2, const double r[4]) {
-  int c1 = rect_code(x1, y1, r), c2 = rect_code(x2, y2, r);
-  for (int guard = 0; guard < 16 && (c1 || c2); guard++) {
-    if (c1 & c2) return false;
-    int c = c1 ? c1 : c2;
-    double x = 0, y = 0;
-    if (c & 1) { y = y1 + (y2 - y1) * (r[0] - x1) / (x2 - x1); x = r[0]; }
-    else if (c & 2) { y = y1 + (y2 - y1) * (r[2] - x1) / (x2 - x1); x = r[2]; }
-    else if (c & 4) { x = x1 + (x2 - x1) * (r[1] - y1) / (y2 - y1); y = r[1]; }
-    else if (c & 8) { x = x1 + (x2 - x1) * (r[3] - y1) / (y2 - y1); y = r[3]; }
-    if (c == c1) { x1 = x; y1 = y; c1 = rect_code(x1, y1, r); }
-    else { x2 = x; y2 = y; c2 = rect_code(x2, y2, r); }
-  }
-  return true;
+// Does the line through the ray's end points S and D meet the outline box
+// [bx0, bx1] x [by0, by1] (FP64)?  The box's centre C lies within its
+// half-width along the line's normal: |cross(D - S, C - S)| <= hx |dy| + hy |dx|
+// (both sides times |D - S|, so no square root or division).  The reference's
+// Cohen-Sutherland clip of the segment S-D (libctsupport/clip.cpp:331-395)
+// keeps exactly the segments whose line does this: both end points lie
+// outside the view circle that holds the box.
+__device__ __forceinline__ bool line_meets_box_fp64(double xs, double ys, double xd, double yd,
+                                                    const PElem& pe) {
+  const double dx = xd - xs, dy = yd - ys;
+  const double hx = 0.5 * (pe.bx1 - pe.bx0), hy = 0.5 * (pe.by1 - pe.by0);
+  const double cx = 0.5 * (pe.bx0 + pe.bx1) - xs, cy = 0.5 * (pe.by0 + pe.by1) - ys;
+  return fabs(dx * cy - dy * cx) <= hx * fabs(dy) + hy * fabs(dx);
 }
 
 // FP32 test of the infinite ray line against the element's outline box:
@@ -189,6 +184,42 @@ __device__ __forceinline__ int box_test(float hx, float hy, float rhob, float rx
   if (m > margin) return 1;
   if (m < -margin) return -1;
   return 0;
+}
+
+// FP64 1/sqrt(x) (x > 0) and 1/x (|x| in [1e-300, 1e300]): the hardware's
+// approximate FP64 estimate (PTX rsqrt.approx.f64 / rcp.approx.f64, about
+// 2^-22 relative) and one Newton-Raphson step, relative error about 1e-13 --
+// a few FP64 operations where the library's correctly rounded forms take
+// tens, at 1/64 of the FP32 rate on this GPU.
+__device__ __forceinline__ double rsqrt_nr(double x) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  return y * fma(-0.5 * x * y, y, 1.5);
+}
+__device__ __forceinline__ double rcp_nr(double x) {
+  if (!(fabs(x) > 1e-300 && fabs(x) < 1e300)) return 1.0 / x;
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  return fma(y, fma(-x, y, 1.0), y);
+}
+
+// atan2(s, c) in FP64 for c >= |s| (angles within pi/4 of the +x axis) by the
+// table-driven method: with z = |s|/c and j the nearest of 64 z,
+// atan z = atan(j/64) + atan r, r = (z - j/64) / (1 + z j/64), |r| <= 1/128
+// (to within the FP32 choice of j), and atan r by its Taylor series to r^7
+// (truncation below 2e-20).  tab[j] = atan(j/64) comes from the host's FP64
+// atan.  Other arguments take the library's atan2.
+__device__ __forceinline__ double atan2_tab(double s, double c, const double* tab) {
+  const double as = fabs(s);
+  if (!(c > 0.0 && as <= c && c < 1e30)) return atan2(s, c);
+  int j = __float2int_rn(64.f * __fdividef((float)as, (float)c));
+  j = min(max(j, 0), 64);
+  const double tj = j * (1.0 / 64.0);
+  const double r = fma(-c, tj, as) * rcp_nr(fma(as, tj, c));
+  const double r2 = r * r;
+  const double p = fma(fma(r2, -1.0 / 7.0, 1.0 / 5.0), r2, -1.0 / 3.0);
+  const double a = tab[j] + fma(p * r2, r, r);
+  return s < 0.0 ? -a : a;
 }
 
 __device__ __forceinline__ void split_root(double t, int& ti, float& tf) {
@@ -212,23 +243,30 @@ __device__ void ray_range(const RaysumLaunch& L, const RayView& g, const PElem& 
   const int kAll = 1 << 30;
   e.tlo = -kAll;
   e.thi = kAll;
-  const double Bx = pe.cx + (double)pe.dcbx, By = pe.cy + (double)pe.dcby;
-  const double R = 1.0001 * (double)pe.rbox + 1e-4 * (fabs(pe.dcbx) + fabs(pe.dcby)) + 1e-30;
-  double t1, t2;
   if (GEOM == kParallel) {
+    const double Bx = pe.cx + (double)pe.dcbx, By = pe.cy + (double)pe.dcby;
+    const double R = 1.0001 * (double)pe.rbox + 1e-4 * (fabs(pe.dcbx) + fabs(pe.dcby)) + 1e-30;
     double rx = (g.D0x + sub * g.dDx) - g.S0x, ry = (g.D0y + sub * g.dDy) - g.S0y;
-    const double inv = 1.0 / sqrt(rx * rx + ry * ry);
+    const double inv = rsqrt_nr(rx * rx + ry * ry);
     rx *= inv;
     ry *= inv;
     const double A = cross2(rx, ry, Bx - g.S0x, By - g.S0y), B = cross2(rx, ry, g.dSx, g.dSy);
     if (B == 0.0) return;
-    t1 = (A - R) / B;
-    t2 = (A + R) / B;
+    const double iB = rcp_nr(B), t1 = (A - R) * iB, t2 = (A + R) * iB;
+    const double pad = 2.0 + 1e-5 * (fabs(t1) + fabs(t2));
+    double lo = fmin(t1, t2) - pad, hi = fmax(t1, t2) + pad;
+    if (!(lo == lo) || !(hi == hi)) return;
+    lo = fmax(lo, -(double)kAll);
+    hi = fmin(hi, (double)kAll);
+    e.tlo = (int)floor(lo);
+    e.thi = (int)ceil(hi);
   } else {
-    const float wx = (float)(Bx - g.S0x), wy = (float)(By - g.S0y);
+    // fan beams in FP32 (the bounds only have to contain the rays)
+    const float R = 1.0001f * pe.rbox + 1e-4f * (fabsf(pe.dcbx) + fabsf(pe.dcby)) + 1e-30f;
+    const float wx = (float)(pe.cx - g.S0x) + pe.dcbx, wy = (float)(pe.cy - g.S0y) + pe.dcby;
     const float dist = sqrtf(wx * wx + wy * wy);
-    if (!(dist > 1.01f * (float)R)) return;
-    const float sb = (float)R / dist;
+    if (!(dist > 1.01f * R)) return;
+    const float sb = R / dist;
     const float cb = sqrtf(1.f - sb * sb);
     const float ux[2] = {(wx * cb - wy * sb) / dist, (wx * cb + wy * sb) / dist};
     const float uy[2] = {(wy * cb + wx * sb) / dist, (wy * cb - wx * sb) / dist};
@@ -252,21 +290,19 @@ __device__ void ray_range(const RaysumLaunch& L, const RayView& g, const PElem& 
         if (!(disc >= 0.f)) return;
         const float lam = -su + sqrtf(disc);
         const float Dx = Sx + lam * ux[k], Dy = Sy + lam * uy[k];
-        const float cm = (float)g.cm, sm = (float)g.sm;
-        tt[k] = (atan2f(cm * Dy - sm * Dx, cm * Dx + sm * Dy) + (float)g.midRel) *
-                (float)g.invDelta;
+        const float cm = g.cmf, sm = g.smf;
+        tt[k] = (atan2f(cm * Dy - sm * Dx, cm * Dx + sm * Dy) + g.midRelf) * g.invDeltaf;
       }
     }
-    t1 = tt[0];
-    t2 = tt[1];
+    // the FP32 pad also covers the rounding of lo and hi themselves
+    const float pad = 2.f + 1e-5f * (fabsf(tt[0]) + fabsf(tt[1]));
+    float lo = fminf(tt[0], tt[1]) - pad, hi = fmaxf(tt[0], tt[1]) + pad;
+    if (!(lo == lo) || !(hi == hi)) return;
+    lo = fmaxf(lo, -(float)kAll);
+    hi = fminf(hi, (float)kAll);
+    e.tlo = (int)floorf(lo);
+    e.thi = (int)ceilf(hi);
   }
-  const double pad = 2.0 + 1e-5 * (fabs(t1) + fabs(t2));
-  double lo = fmin(t1, t2) - pad, hi = fmax(t1, t2) + pad;
-  if (!(lo == lo) || !(hi == hi)) return;
-  lo = fmax(lo, -(double)kAll);
-  hi = fmin(hi, (double)kAll);
-  e.tlo = (int)floor(lo);
-  e.thi = (int)ceil(hi);
 }
 
 // FP64 set-up of one (view, element[, ray sample]) record.
@@ -285,14 +321,10 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
   e.hy = pe.hy;
   e.rbox = pe.rbox;
   e.rin = pe.rin;
-  {
-    const double iu2 = 1.0 / (pe.u * pe.u), iv2 = 1.0 / (pe.v * pe.v);
-    const double c = pe.cosr, sn = pe.sinr;
-    e.qa = (float)(c * c * iu2 + sn * sn * iv2);
-    e.qb = (float)(2.0 * c * sn * (iu2 - iv2));
-    e.qc = (float)(sn * sn * iu2 + c * c * iv2);
-    e.uv = e.u * e.v;
-  }
+  e.qa = pe.qa;
+  e.qb = pe.qb;
+  e.qc = pe.qc;
+  e.uv = pe.uv;
   e.cpsi = e.spsi = 0.f;
   e.ra = e.rb = 0.f;
   e.kB = 0.f;
@@ -305,14 +337,14 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
   if (GEOM == kParallel) {
     // ray direction of sub-sample `sub` (independent of the detector index)
     double rx = (g.D0x + sub * g.dDx) - g.S0x, ry = (g.D0y + sub * g.dDy) - g.S0y;
-    double inv = 1.0 / sqrt(rx * rx + ry * ry);
+    double inv = rsqrt_nr(rx * rx + ry * ry);
     rx *= inv;
     ry *= inv;
     double wx = pe.cx - g.S0x, wy = pe.cy - g.S0y;
     double A = cross2(rx, ry, wx, wy), B = cross2(rx, ry, g.dSx, g.dSy);
     // rho(d) = A - d B
     if (B == 0.0) return;
-    split_root(A / B, e.tcI, e.tcF);
+    split_root(A * rcp_nr(B), e.tcI, e.tcF);
     e.kB = (float)(-B);
     e.ra = (float)(rx * pe.cosr + ry * pe.sinr);
     e.rb = (float)(-rx * pe.sinr + ry * pe.cosr);
@@ -321,7 +353,7 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
     double A = cross2(g.D0x - g.S0x, g.D0y - g.S0y, wx, wy);
     double B = cross2(g.dDx, g.dDy, wx, wy);
     if (B == 0.0) return;
-    split_root(-A / B, e.tcI, e.tcF);
+    split_root(-A * rcp_nr(B), e.tcI, e.tcF);
     e.kB = (float)B;
   } else {
     // The arc point D(a) = CD (cos a, sin a) sees the element centre W from the
@@ -333,21 +365,28 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
     // which is the reference's branch choice without an arcsine.
     const double CD = L.centerDetectorLength;
     const double wx = pe.cx - g.S0x, wy = pe.cy - g.S0y;
-    const double wn = sqrt(wx * wx + wy * wy);
-    const double q = cross2(g.S0x, g.S0y, wx, wy) / (CD * wn);
+    const double w2 = wx * wx + wy * wy;
+    const double iw = rsqrt_nr(w2), wn = w2 * iw;
+    const double q = cross2(g.S0x, g.S0y, wx, wy) * iw * L.invCD;
     if (!(fabs(q) <= 1.0)) return;
-    const double cb = sqrt((1.0 - q) * (1.0 + q));
-    const double iw = 1.0 / wn;
-    const double u1x = (wx * cb + wy * q) * iw, u1y = (wy * cb - wx * q) * iw;
-    const double u2x = -(wx * cb - wy * q) * iw, u2y = -(wy * cb + wx * q) * iw;
-    const double d1 = u1x * g.cm + u1y * g.sm, d2 = u2x * g.cm + u2y * g.sm;
-    const double ux = d1 >= d2 ? u1x : u2x, uy = d1 >= d2 ? u1y : u2y;
-    const double rel = atan2(g.cm * uy - g.sm * ux, g.cm * ux + g.sm * uy) + g.midRel;
+    const double cb2 = (1.0 - q) * (1.0 + q);
+    const double cb = cb2 > 1e-300 ? cb2 * rsqrt_nr(cb2) : sqrt(cb2);
+    // of the solutions u1 = ((wx cb + wy q), (wy cb - wx q)) / |w| and
+    // u2 = -((wx cb - wy q), (wy cb + wx q)) / |w|, the one nearer the arc's
+    // middle, chosen in FP32 (the two are far apart for any element whose rays
+    // reach the detector) and built in FP64
+    const float wxf = (float)wx, wyf = (float)wy, cbf = (float)cb, qf = (float)q;
+    const float d1 = fmaf(wxf, cbf, wyf * qf) * g.cmf + fmaf(wyf, cbf, -wxf * qf) * g.smf;
+    const float d2 = -fmaf(wxf, cbf, -wyf * qf) * g.cmf - fmaf(wyf, cbf, wxf * qf) * g.smf;
+    const double sg = d1 >= d2 ? 1.0 : -1.0;
+    const double ux = sg * (wx * cb + sg * wy * q) * iw, uy = sg * (wy * cb - sg * wx * q) * iw;
+    const double rel =
+        atan2_tab(g.cm * uy - g.sm * ux, g.cm * ux + g.sm * uy, L.atan64) + g.midRel;
     split_root(rel * g.invDelta, e.tcI, e.tcF);
     e.kB = (float)(2.0 * CD * wn);
     // psi = theta_w - (a + alpha0)/2 = (theta_w - alpha0) - rel/2 enters only
     // through its cosine and sine: FP32
-    const float thw0 = atan2f((float)(g.c0 * wy - g.s0 * wx), (float)(g.c0 * wx + g.s0 * wy));
+    const float thw0 = atan2f(g.ca0 * wyf - g.sa0 * wxf, g.ca0 * wxf + g.sa0 * wyf);
     float sp, cp;
     sincosf(thw0 - 0.5f * (float)rel, &sp, &cp);
     e.cpsi = cp;
@@ -481,16 +520,15 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
         const float4 w4 = ld4(&e.hx);     // hx, hy, atten, tcI
         int bt = arhob < w2.z ? 1 : box_test(w4.x, w4.y, rhob, rx, ry);
         if (bt == 0) {
-          // repeat the reference's FP64 box clip on this ray's end points
+          // within the FP32 test's margin: decide in FP64 on this ray's end
+          // points whether its line meets the outline box
           const PElem& pe = elems[k];
-          double lim[4] = {pe.bx0, pe.by0, pe.bx1, pe.by1};
           double xd, yd, xs, ys;
           if (GEOM == kEquiangular) {
-            double a = g.alpha0 + (double)t * g.delta;
-            double sa, ca;
-            sincos(a, &sa, &ca);
-            xd = L.centerDetectorLength * ca;
-            yd = L.centerDetectorLength * sa;
+            // detector point at arc angle alpha0 + t delta, by the angle sum
+            const double2 a = L.arc[t];
+            xd = L.centerDetectorLength * (g.c0 * a.x - g.s0 * a.y);
+            yd = L.centerDetectorLength * (g.s0 * a.x + g.c0 * a.y);
             xs = g.S0x;
             ys = g.S0y;
           } else {
@@ -500,7 +538,7 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
             xd = g.D0x + (double)tt * g.dDx;
             yd = g.D0y + (double)tt * g.dDy;
           }
-          bt = clip_rect_fp64(xd, yd, xs, ys, lim) ? 1 : -1;
+          bt = line_meets_box_fp64(xs, ys, xd, yd, pe) ? 1 : -1;
         }
         if (bt < 0) continue;
         sum = fmaf(ch, w4.z, sum);
@@ -540,8 +578,21 @@ static cudaError_t raysum_launch(const RaysumLaunch& L, size_t smem, int nSlices
   return cudaGetLastError();
 }
 
-cudaError_t launch_raysum(const RaysumLaunch& L, cudaStream_t s) {
-  if (L.nViews <= 0) return cudaSuccess;
+// atan(j / 64), j = 0..64, by the host's FP64 atan
+static const std::array<double, 65>& atan64_table() {
+  static const std::array<double, 65> tab = [] {
+    std::array<double, 65> t{};
+    for (int j = 0; j <= 64; j++) t[j] = std::atan(j / 64.0);
+    return t;
+  }();
+  return tab;
+}
+
+cudaError_t launch_raysum(const RaysumLaunch& L0, cudaStream_t s) {
+  if (L0.nViews <= 0) return cudaSuccess;
+  RaysumLaunch L = L0;
+  L.invCD = L.centerDetectorLength != 0.0 ? 1.0 / L.centerDetectorLength : 0.0;
+  std::copy(atan64_table().begin(), atan64_table().end(), L.atan64);
   int nSub = (L.geometry == kParallel) ? L.nSample : 1;
   size_t smem = dir_table_offset((L.nElem > 0 ? L.nElem : 1) * nSub) +
                 sizeof(float2) * (size_t)L.nSample;
@@ -579,6 +630,7 @@ __global__ void ellipsoid_section_kernel(const PElem* base, const double2* zc, i
     e.hy = (float)hy;
     e.rbox = (float)(sqrt(hx * hx + hy * hy) * (1.0 + 1e-5) + 1e-7);
     e.rin = (float)(fmin(hx, hy) - 2e-5 * (hx + hy) - 1e-7);
+    set_elem_quadratic(e);
   }
   out[idx] = e;
 }
@@ -671,7 +723,6 @@ __global__ void __launch_bounds__(128) raysum_ellipse_grad_kernel(RaysumLaunch L
     const double ct = pe.cosr, st = pe.sinr, at = pe.atten;
     const double bcx = 0.5 * (pe.bx0 + pe.bx1), bcy = 0.5 * (pe.by0 + pe.by1);
     const double rin = fmin(pe.bx1 - pe.bx0, pe.by1 - pe.by0) * 0.5 * (1.0 - 1e-9);
-    const double lim[4] = {pe.bx0, pe.by0, pe.bx1, pe.by1};
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int t = threadIdx.x; t < nRay; t += blockDim.x) {
       const GradRay R = rays[t];
@@ -681,9 +732,9 @@ __global__ void __launch_bounds__(128) raysum_ellipse_grad_kernel(RaysumLaunch L
       const double h2 = Q - rho * rho;
       if (!(h2 > 0.0)) continue;
       // the forward model's outline-box acceptance: certain inside the box's
-      // inscribed circle, else the reference's clip on the ray's end points
+      // inscribed circle, else the FP64 line-box test on the ray's end points
       const double rbox = R.rx * (bcy - R.sy) - R.ry * (bcx - R.sx);
-      if (!(fabs(rbox) < rin) && !clip_rect_fp64(R.xd, R.yd, R.sx, R.sy, lim)) continue;
+      if (!(fabs(rbox) < rin) && !line_meets_box_fp64(R.sx, R.sy, R.xd, R.yd, pe)) continue;
       const double hc = sqrt(h2);
       const double iQ = 1.0 / Q;
       const double c = 2.0 * u * v * hc * iQ;
