@@ -230,26 +230,42 @@ __device__ __forceinline__ void split_root(double t, int& ti, float& tf) {
   tf = (float)(t - fl);
 }
 
-// Ray indices whose lines can come within the outline box's circumcircle
-// (centre B, radius rbox): an early-out ahead of the rays' exact test, so it
-// only has to contain them -- FP32 tangents from the source, widened by two
-// rays.  Parallel rays: |rho_B(d)| = |A - d B| <= rbox is an interval.  Fan
-// rays: the two tangents from the source to the circle, mapped to ray
-// indices (detector line or arc).  The radius is widened well past the FP32
-// rounding of the rays' own distance test (a few ulp of |rho| + |dcb|).
+// Ray indices whose lines can meet the element: an early-out ahead of the
+// rays' exact test, so it only has to contain them -- tangents from the
+// source, widened by two rays.  An ellipse's rays are those that meet the
+// ellipse itself (a ray with a chord does); other elements' those within the
+// outline box's circumcircle (centre B, radius rbox).  Parallel rays:
+// |rho_B(d)| = |A - d B| <= R is an interval.  Fan rays: the two tangents from
+// the source, mapped to ray indices (detector line or arc).  The radius is
+// widened well past the FP32 rounding of the rays' own tests.
 template <int GEOM>
 __device__ void ray_range(const RaysumLaunch& L, const RayView& g, const PElem& pe, int sub,
                           ElemView& e) {
   const int kAll = 1 << 30;
   e.tlo = -kAll;
   e.thi = kAll;
+  const bool ell = pe.type == kEllipse;
   if (GEOM == kParallel) {
-    const double Bx = pe.cx + (double)pe.dcbx, By = pe.cy + (double)pe.dcby;
-    const double R = 1.0001 * (double)pe.rbox + 1e-4 * (fabs(pe.dcbx) + fabs(pe.dcby)) + 1e-30;
     double rx = (g.D0x + sub * g.dDx) - g.S0x, ry = (g.D0y + sub * g.dDy) - g.S0y;
     const double inv = rsqrt_nr(rx * rx + ry * ry);
     rx *= inv;
     ry *= inv;
+    // the lines within R of the point B: an ellipse's own centre and its
+    // half-width across the rays, sqrt(u^2 (n.a1)^2 + v^2 (n.a2)^2) for the
+    // rays' normal n and the element axes a1, a2; other elements the outline
+    // box's circumcircle
+    double Bx, By, R;
+    if (ell) {
+      const double na1 = rx * pe.sinr - ry * pe.cosr, na2 = rx * pe.cosr + ry * pe.sinr;
+      const double h2 = pe.u * pe.u * na1 * na1 + pe.v * pe.v * na2 * na2;
+      Bx = pe.cx;
+      By = pe.cy;
+      R = 1.0001 * (h2 * rsqrt_nr(h2)) + 1e-6;
+    } else {
+      Bx = pe.cx + (double)pe.dcbx;
+      By = pe.cy + (double)pe.dcby;
+      R = 1.0001 * (double)pe.rbox + 1e-4 * (fabs(pe.dcbx) + fabs(pe.dcby)) + 1e-30;
+    }
     const double A = cross2(rx, ry, Bx - g.S0x, By - g.S0y), B = cross2(rx, ry, g.dSx, g.dSy);
     if (B == 0.0) return;
     const double iB = rcp_nr(B), t1 = (A - R) * iB, t2 = (A + R) * iB;
@@ -261,15 +277,42 @@ __device__ void ray_range(const RaysumLaunch& L, const RayView& g, const PElem& 
     e.tlo = (int)floor(lo);
     e.thi = (int)ceil(hi);
   } else {
-    // fan beams in FP32 (the bounds only have to contain the rays)
-    const float R = 1.0001f * pe.rbox + 1e-4f * (fabsf(pe.dcbx) + fabsf(pe.dcby)) + 1e-30f;
-    const float wx = (float)(pe.cx - g.S0x) + pe.dcbx, wy = (float)(pe.cy - g.S0y) + pe.dcby;
-    const float dist = sqrtf(wx * wx + wy * wy);
-    if (!(dist > 1.01f * R)) return;
-    const float sb = R / dist;
-    const float cb = sqrtf(1.f - sb * sb);
-    const float ux[2] = {(wx * cb - wy * sb) / dist, (wx * cb + wy * sb) / dist};
-    const float uy[2] = {(wy * cb + wx * sb) / dist, (wy * cb - wx * sb) / dist};
+    // fan beams in FP32 (the bounds only have to contain the rays): the two
+    // tangents from the source
+    float ux[2], uy[2];
+    if (ell) {
+      // to the ellipse itself: in the element frame scaled to the unit circle
+      // the source sits at p, the tangent points at angle(p) +- acos(1/|p|)
+      const float ct = (float)pe.cosr, st = (float)pe.sinr, eu = (float)pe.u, ev = (float)pe.v;
+      const float dxs = (float)(g.S0x - pe.cx), dys = (float)(g.S0y - pe.cy);
+      const float px = (ct * dxs + st * dys) / eu, py = (ct * dys - st * dxs) / ev;
+      const float pn2 = px * px + py * py;
+      if (!(pn2 > 1.0201f)) return;   // the source within 1.01 of the ellipse's size
+      const float ip = rsqrtf(pn2);
+      const float ca = ip, sa = sqrtf(fmaxf(0.f, 1.f - ip * ip));
+      const float qx = px * ip, qy = py * ip;
+      for (int k = 0; k < 2; k++) {
+        const float sg = k ? -1.f : 1.f;
+        const float tx = qx * ca - sg * qy * sa, ty = qy * ca + sg * qx * sa;
+        // tangent point minus source, back in the world frame
+        const float ex = ct * eu * tx - st * ev * ty - dxs, ey = st * eu * tx + ct * ev * ty - dys;
+        const float il = rsqrtf(ex * ex + ey * ey);
+        ux[k] = ex * il;
+        uy[k] = ey * il;
+      }
+    } else {
+      // to the outline box's circumcircle
+      const float R = 1.0001f * pe.rbox + 1e-4f * (fabsf(pe.dcbx) + fabsf(pe.dcby)) + 1e-30f;
+      const float wx = (float)(pe.cx - g.S0x) + pe.dcbx, wy = (float)(pe.cy - g.S0y) + pe.dcby;
+      const float dist = sqrtf(wx * wx + wy * wy);
+      if (!(dist > 1.01f * R)) return;
+      const float sb = R / dist;
+      const float cb = sqrtf(1.f - sb * sb);
+      ux[0] = (wx * cb - wy * sb) / dist;
+      ux[1] = (wx * cb + wy * sb) / dist;
+      uy[0] = (wy * cb + wx * sb) / dist;
+      uy[1] = (wy * cb - wx * sb) / dist;
+    }
     float tt[2];
     if (GEOM == kEquilinear) {
       // both tangents must meet the detector line on the same side
