@@ -529,62 +529,81 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
         rx *= invr;
         ry *= invr;
       }
-      for (int k = 0; k < nElem; k++) {
-        const ElemView& e = ev[k * nSub + (GEOM == kParallel ? i : 0)];
-        const int4 hdr = *reinterpret_cast<const int4*>(&e);
-        if (t < hdr.x || t > hdr.y) continue;
-        // integers below 2^24: (float)tcI - ft is the exact (float)(tcI - t)
-        const float ftc = __int_as_float(hdr.z), tcF = __int_as_float(hdr.w);
-        const float4 w1 = ld4(&e.kB);     // kB, cpsi, spsi, rbox
-        float rho;
-        if (GEOM == kEquiangular) {
-          float x = ((ftc - ft) + tcF) * hdelta;
-          float cf = fmaf(w1.y, cj, w1.z * sj);
-          rho = w1.x * cf * sin_series(x) * invr;
-        } else {
-          float dt = (ft - ftc) - tcF;
-          rho = w1.x * dt * invr;
+      // the elements whose ray range meets this warp's rays: lane j tests
+      // element kb + j, a ballot collects them, and the loop visits them in
+      // ascending order (the sums keep their order).  The warp's lanes in this
+      // iteration are the detectors dw0 .. dwm, all of them here.
+      const int dw0 = d - (int)(threadIdx.x & 31), dwm = min(dw0 + 31, L.nDet - 1);
+      const unsigned wmask = dwm - dw0 >= 31 ? 0xffffffffu : (1u << (dwm - dw0 + 1)) - 1u;
+      const int twlo = (GEOM == kParallel) ? dw0 : dw0 * nS + i;
+      const int twhi = (GEOM == kParallel) ? dwm : dwm * nS + i;
+      for (int kb = 0; kb < nElem; kb += 32) {
+        const int kl = kb + (int)(threadIdx.x & 31);
+        bool meets = false;
+        if (kl < nElem) {
+          const int2 r = *reinterpret_cast<const int2*>(&ev[kl * nSub + (GEOM == kParallel ? i : 0)]);
+          meets = !(twhi < r.x || twlo > r.y);
         }
-        // cull against the outline box's circumcircle
-        const float4 w2 = ld4(&e.dcbx);   // dcbx, dcby, rin, type
-        float rhob = rho + (rx * w2.y - ry * w2.x);
-        const float arhob = fabsf(rhob);
-        if (arhob > w1.w) continue;
-        float ch;
-        if (__float_as_int(w2.w) == kEllipse) {
-          ch = ellipse_chord(ld4(&e.qa), rho, rx, ry);
-        } else {
-          float ra, rb;
-          if (GEOM == kParallel) { ra = e.ra; rb = e.rb; }
-          else { ra = rx * e.ca + ry * e.sa; rb = -rx * e.sa + ry * e.ca; }
-          ch = element_chord(e, rho, rx, ry, ra, rb);
-        }
-        if (ch <= 0.f) continue;
-        const float4 w4 = ld4(&e.hx);     // hx, hy, atten, tcI
-        int bt = arhob < w2.z ? 1 : box_test(w4.x, w4.y, rhob, rx, ry);
-        if (bt == 0) {
-          // within the FP32 test's margin: decide in FP64 on this ray's end
-          // points whether its line meets the outline box
-          const PElem& pe = elems[k];
-          double xd, yd, xs, ys;
+        unsigned todo = __ballot_sync(wmask, meets);
+        while (todo) {
+          const int k = kb + __ffs(todo) - 1;
+          todo &= todo - 1;
+          const ElemView& e = ev[k * nSub + (GEOM == kParallel ? i : 0)];
+          const int4 hdr = *reinterpret_cast<const int4*>(&e);
+          if (t < hdr.x || t > hdr.y) continue;
+          // integers below 2^24: (float)tcI - ft is the exact (float)(tcI - t)
+          const float ftc = __int_as_float(hdr.z), tcF = __int_as_float(hdr.w);
+          const float4 w1 = ld4(&e.kB);     // kB, cpsi, spsi, rbox
+          float rho;
           if (GEOM == kEquiangular) {
-            // detector point at arc angle alpha0 + t delta, by the angle sum
-            const double2 a = L.arc[t];
-            xd = L.centerDetectorLength * (g.c0 * a.x - g.s0 * a.y);
-            yd = L.centerDetectorLength * (g.s0 * a.x + g.c0 * a.y);
-            xs = g.S0x;
-            ys = g.S0y;
+            float x = ((ftc - ft) + tcF) * hdelta;
+            float cf = fmaf(w1.y, cj, w1.z * sj);
+            rho = w1.x * cf * sin_series(x) * invr;
           } else {
-            xs = g.S0x + (GEOM == kParallel ? d * g.dSx : 0.0);
-            ys = g.S0y + (GEOM == kParallel ? d * g.dSy : 0.0);
-            int tt = d * nS + i;
-            xd = g.D0x + (double)tt * g.dDx;
-            yd = g.D0y + (double)tt * g.dDy;
+            float dt = (ft - ftc) - tcF;
+            rho = w1.x * dt * invr;
           }
-          bt = line_meets_box_fp64(xs, ys, xd, yd, pe) ? 1 : -1;
+          // cull against the outline box's circumcircle
+          const float4 w2 = ld4(&e.dcbx);   // dcbx, dcby, rin, type
+          float rhob = rho + (rx * w2.y - ry * w2.x);
+          const float arhob = fabsf(rhob);
+          if (arhob > w1.w) continue;
+          float ch;
+          if (__float_as_int(w2.w) == kEllipse) {
+            ch = ellipse_chord(ld4(&e.qa), rho, rx, ry);
+          } else {
+            float ra, rb;
+            if (GEOM == kParallel) { ra = e.ra; rb = e.rb; }
+            else { ra = rx * e.ca + ry * e.sa; rb = -rx * e.sa + ry * e.ca; }
+            ch = element_chord(e, rho, rx, ry, ra, rb);
+          }
+          if (ch <= 0.f) continue;
+          const float4 w4 = ld4(&e.hx);     // hx, hy, atten, tcI
+          int bt = arhob < w2.z ? 1 : box_test(w4.x, w4.y, rhob, rx, ry);
+          if (bt == 0) {
+            // within the FP32 test's margin: decide in FP64 on this ray's end
+            // points whether its line meets the outline box
+            const PElem& pe = elems[k];
+            double xd, yd, xs, ys;
+            if (GEOM == kEquiangular) {
+              // detector point at arc angle alpha0 + t delta, by the angle sum
+              const double2 a = L.arc[t];
+              xd = L.centerDetectorLength * (g.c0 * a.x - g.s0 * a.y);
+              yd = L.centerDetectorLength * (g.s0 * a.x + g.c0 * a.y);
+              xs = g.S0x;
+              ys = g.S0y;
+            } else {
+              xs = g.S0x + (GEOM == kParallel ? d * g.dSx : 0.0);
+              ys = g.S0y + (GEOM == kParallel ? d * g.dSy : 0.0);
+              int tt = d * nS + i;
+              xd = g.D0x + (double)tt * g.dDx;
+              yd = g.D0y + (double)tt * g.dDy;
+            }
+            bt = line_meets_box_fp64(xs, ys, xd, yd, pe) ? 1 : -1;
+          }
+          if (bt < 0) continue;
+          sum = fmaf(ch, w4.z, sum);
         }
-        if (bt < 0) continue;
-        sum = fmaf(ch, w4.z, sum);
       }
     }
     sino[(size_t)(L.rowOffset + view) * L.pitch + d] = sum / fnS;
