@@ -632,8 +632,9 @@ def run_gpu(args):
                                  "peak": fp32_peak, "unit": "TFLOP/s",
                                  "frac": RAYS_PER_SLICE * 12 * B * steps * world * 60 /
                                          (ray_ms / 1e3) / 1e12 / fp32_peak,
-                                 "note": "set-up and ray kernels together; ncu: issue slots "
-                                         "~82 % busy (profiles/raysum_equiangular_733x720_ncu.md)"},
+                                 "note": "set-up and ray kernels together; ncu: ray kernel "
+                                         "issue slots ~89 % busy, set-up FP64 pipe ~70 % busy "
+                                         "(profiles/raysum_equiangular_733x720_ncu.md)"},
                     "cpu_baseline": {"value": cpu_raysum_rate[0], "unit": "ray-sums/s",
                                      "cores": cpu_threads, "kind": "port",
                                      "sample": "one 733 x 720 equiangular scan of 12 ellipses"}},
