@@ -245,12 +245,10 @@ struct ctgpu_scanner {
   size_t d_records_cap = 0;
   float* d_sino = nullptr;
   size_t d_sino_cap = 0;
-  // collect_projections_batch: the phantoms' elements back to back, offsets
+  // collect_projections_ellipsoids: the ellipsoids' largest cross-sections,
+  // the per-view cross-sections, the ellipsoids' z extents
   PElem* d_belems = nullptr;
   size_t d_belems_cap = 0;
-  int* d_boffs = nullptr;
-  size_t d_boffs_cap = 0;
-  // collect_projections_ellipsoids: per-view cross-sections, ellipsoid z extents
   PElem* d_velems = nullptr;
   size_t d_velems_cap = 0;
   double2* d_zc = nullptr;
@@ -262,11 +260,25 @@ struct ctgpu_scanner {
   size_t d_arc_cap = 0;
   int arcN = 0;
   double arcDelta = 0;
+  // collect_projections_batch: the views' ray records, the parallel ray
+  // directions, the phantoms' elements and their offsets go up as one copy
+  // from a page-locked buffer (two, used in turn: the host fills one while
+  // the other's copy may still be queued) to one device buffer
+  unsigned char* h_stage[2] = {nullptr, nullptr};
+  size_t h_stage_cap[2] = {0, 0};
+  cudaEvent_t stage_done[2] = {nullptr, nullptr};
+  int stage_next = 0;
+  unsigned char* d_stage = nullptr;
+  size_t d_stage_cap = 0;
   ~ctgpu_scanner() {
-    for (void* p : {(void*)d_views, (void*)d_sino, (void*)d_belems, (void*)d_boffs,
+    for (void* p : {(void*)d_views, (void*)d_sino, (void*)d_belems,
                     (void*)d_sdirs, (void*)d_records, (void*)d_velems, (void*)d_zc,
-                    (void*)d_arc})
+                    (void*)d_arc, (void*)d_stage})
       if (p) cudaFree(p);
+    for (int b = 0; b < 2; b++) {
+      if (h_stage[b]) cudaFreeHost(h_stage[b]);
+      if (stage_done[b]) cudaEventDestroy(stage_done[b]);
+    }
   }
 };
 
@@ -597,32 +609,13 @@ RayView ctgpu::make_ray_view(int geometry, int nDet, int nS, double angularDetLe
   return g;
 }
 
-// the scanner's current views as ray records (+ parallel ray directions) on the device
-static cudaError_t upload_ray_views(ctgpu_scanner* s, int nViews, cudaStream_t st) {
-  std::vector<RayView> rv(nViews);
+// the scanner's current views as ray records, and for parallel rays their
+// directions ([view][sample]), into host memory
+static void fill_ray_views(const ctgpu_scanner* s, int nViews, RayView* rv, float2* dirs) {
   for (int v = 0; v < nViews; v++)
     rv[v] = make_ray_view(s->geometry, s->nDet, s->nSample, s->angularDetLen, s->angularDetInc,
                           s->views[v]);
-  cudaError_t e = ensure_device(s->d_views, s->d_views_cap, (size_t)nViews);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(s->d_views, rv.data(), sizeof(RayView) * nViews, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return e;
-  if (s->geometry == kEquiangular) {
-    const int n = s->nDet * s->nSample;
-    const double delta = s->angularDetInc / s->nSample;
-    if (s->arcN != n || s->arcDelta != delta) {
-      std::vector<double2> arc(n);
-      for (int t = 0; t < n; t++) arc[t] = make_double2(std::cos(t * delta), std::sin(t * delta));
-      e = ensure_device(s->d_arc, s->d_arc_cap, (size_t)n);
-      if (e == cudaSuccess)
-        e = cudaMemcpy(s->d_arc, arc.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
-      if (e != cudaSuccess) return e;
-      s->arcN = n;
-      s->arcDelta = delta;
-    }
-  }
-  if (s->geometry != kParallel) return e;
-  std::vector<float2> dirs((size_t)nViews * s->nSample);
+  if (s->geometry != kParallel) return;
   for (int v = 0; v < nViews; v++)
     for (int i = 0; i < s->nSample; i++) {
       const RayView& g = rv[v];
@@ -630,6 +623,34 @@ static cudaError_t upload_ray_views(ctgpu_scanner* s, int nViews, cudaStream_t s
       double inv = 1.0 / std::sqrt(drx * drx + dry * dry);
       dirs[(size_t)v * s->nSample + i] = make_float2((float)(drx * inv), (float)(dry * inv));
     }
+}
+
+// equiangular: the scanner's table of (cos, sin) of t * delta (built once)
+static cudaError_t ensure_arc_table(ctgpu_scanner* s) {
+  if (s->geometry != kEquiangular) return cudaSuccess;
+  const int n = s->nDet * s->nSample;
+  const double delta = s->angularDetInc / s->nSample;
+  if (s->arcN == n && s->arcDelta == delta) return cudaSuccess;
+  std::vector<double2> arc(n);
+  for (int t = 0; t < n; t++) arc[t] = make_double2(std::cos(t * delta), std::sin(t * delta));
+  cudaError_t e = ensure_device(s->d_arc, s->d_arc_cap, (size_t)n);
+  if (e == cudaSuccess) e = cudaMemcpy(s->d_arc, arc.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return e;
+  s->arcN = n;
+  s->arcDelta = delta;
+  return cudaSuccess;
+}
+
+// the scanner's current views as ray records (+ parallel ray directions) on the device
+static cudaError_t upload_ray_views(ctgpu_scanner* s, int nViews, cudaStream_t st) {
+  std::vector<RayView> rv(nViews);
+  std::vector<float2> dirs(s->geometry == kParallel ? (size_t)nViews * s->nSample : 0);
+  fill_ray_views(s, nViews, rv.data(), dirs.data());
+  cudaError_t e = ensure_device(s->d_views, s->d_views_cap, (size_t)nViews);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->d_views, rv.data(), sizeof(RayView) * nViews, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = ensure_arc_table(s);
+  if (e != cudaSuccess || s->geometry != kParallel) return e;
   e = ensure_device(s->d_sdirs, s->d_sdirs_cap, dirs.size());
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(s->d_sdirs, dirs.data(), sizeof(float2) * dirs.size(),
@@ -703,14 +724,33 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   scanner_views(s, 0, s->nView, 0);
   if (h_angles)
     for (int v = 0; v < s->nView; v++) h_angles[v] = s->views[v].angle;
-  CUDA_TRY(ensure_device(s->d_belems, s->d_belems_cap, all.size()));
-  CUDA_TRY(ensure_device(s->d_boffs, s->d_boffs_cap, offs.size()));
-  CUDA_TRY(upload_ray_views(s, s->nView, st));
-  if (!all.empty())
-    CUDA_TRY(cudaMemcpyAsync(s->d_belems, all.data(), sizeof(PElem) * all.size(),
-                             cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(s->d_boffs, offs.data(), sizeof(int) * offs.size(),
-                           cudaMemcpyHostToDevice, st));
+  CUDA_TRY(ensure_arc_table(s));
+  // one staging buffer: [ray records][parallel directions][elements][offsets]
+  const int nv = s->nView;
+  const bool par = s->geometry == kParallel;
+  auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  const size_t oD = up16(sizeof(RayView) * nv);
+  const size_t oE = up16(oD + (par ? sizeof(float2) * nv * s->nSample : 0));
+  const size_t oO = up16(oE + sizeof(PElem) * all.size());
+  const size_t total = oO + sizeof(int) * offs.size();
+  const int b = s->stage_next;
+  s->stage_next ^= 1;
+  if (s->stage_done[b]) CUDA_TRY(cudaEventSynchronize(s->stage_done[b]));   // its last copy
+  else CUDA_TRY(cudaEventCreateWithFlags(&s->stage_done[b], cudaEventDisableTiming));
+  if (s->h_stage_cap[b] < total) {
+    if (s->h_stage[b]) cudaFreeHost(s->h_stage[b]);
+    s->h_stage[b] = nullptr;
+    s->h_stage_cap[b] = 0;
+    CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&s->h_stage[b]), total, cudaHostAllocDefault));
+    s->h_stage_cap[b] = total;
+  }
+  unsigned char* h = s->h_stage[b];
+  fill_ray_views(s, nv, reinterpret_cast<RayView*>(h), reinterpret_cast<float2*>(h + oD));
+  if (!all.empty()) std::memcpy(h + oE, all.data(), sizeof(PElem) * all.size());
+  std::memcpy(h + oO, offs.data(), sizeof(int) * offs.size());
+  CUDA_TRY(ensure_device(s->d_stage, s->d_stage_cap, total));
+  CUDA_TRY(cudaMemcpyAsync(s->d_stage, h, total, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaEventRecord(s->stage_done[b], st));
   RaysumLaunch L{};
   L.geometry = s->geometry;
   L.nDet = s->nDet;
@@ -722,14 +762,14 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   L.centerDetectorLength = s->centerDetectorLength;
   L.angularDetLen = s->angularDetLen;
   L.angularDetInc = s->angularDetInc;
-  L.elems = s->d_belems;
-  L.views = s->d_views;
-  L.sdirs = s->d_sdirs;
+  L.elems = reinterpret_cast<const PElem*>(s->d_stage + oE);
+  L.views = reinterpret_cast<const RayView*>(s->d_stage);
+  L.sdirs = par ? reinterpret_cast<const float2*>(s->d_stage + oD) : nullptr;
   L.arc = s->d_arc;
   L.sino = d_sinos;
   L.status = status_pointer();
   L.nSlices = n;
-  L.elemOffset = s->d_boffs;
+  L.elemOffset = reinterpret_cast<const int*>(s->d_stage + oO);
   L.sliceStride = (size_t)sliceStride;
   CUDA_TRY(ensure_device(s->d_records, s->d_records_cap, raysum_record_bytes(L, (int)all.size())));
   L.records = s->d_records;
