@@ -237,6 +237,8 @@ struct ctgpu_scanner {
   double xs1, ys1, xs2, ys2, xd1 = 0, yd1 = 0, xd2 = 0, yd2 = 0;
   M3 inc;
   std::vector<ViewPos> views;
+  // collect_projections_ellipsoids, raysum_ellipse_gradient: the views' ray
+  // records and parallel directions
   RayView* d_views = nullptr;
   size_t d_views_cap = 0;
   float2* d_sdirs = nullptr;
@@ -260,16 +262,21 @@ struct ctgpu_scanner {
   size_t d_arc_cap = 0;
   int arcN = 0;
   double arcDelta = 0;
-  // collect_projections_batch: the views' ray records, the parallel ray
-  // directions, the phantoms' elements and their offsets go up as one copy
-  // from a page-locked buffer (two, used in turn: the host fills one while
-  // the other's copy may still be queued) to one device buffer
+  // the ray-sum calls' per-call inputs (the views' ray records, parallel ray
+  // directions, elements, offsets) go up as one copy from a page-locked
+  // buffer (two, used in turn: the host fills one while the other's copy may
+  // still be queued) to one device buffer
   unsigned char* h_stage[2] = {nullptr, nullptr};
   size_t h_stage_cap[2] = {0, 0};
   cudaEvent_t stage_done[2] = {nullptr, nullptr};
   int stage_next = 0;
   unsigned char* d_stage = nullptr;
   size_t d_stage_cap = 0;
+  // ray records and directions are built here, in ordinary host memory, and
+  // moved into the page-locked buffer with one bulk copy (record-by-record
+  // stores into page-locked memory were slower on the Arm hosts)
+  std::vector<RayView> h_rv;
+  std::vector<float2> h_dirs;
   ~ctgpu_scanner() {
     for (void* p : {(void*)d_views, (void*)d_sino, (void*)d_belems,
                     (void*)d_sdirs, (void*)d_records, (void*)d_velems, (void*)d_zc,
@@ -658,6 +665,46 @@ static cudaError_t upload_ray_views(ctgpu_scanner* s, int nViews, cudaStream_t s
   return e;
 }
 
+// The scanner's page-locked staging buffer (two, used in turn) for `total`
+// bytes, after its last copy is done: the host fills it, stage_send sends it
+// to s->d_stage in one asynchronous copy on st.  Copies from pageable memory
+// block the host and each sits in the stream as its own transfer.
+static cudaError_t stage_host(ctgpu_scanner* s, size_t total, unsigned char** h, int* slot) {
+  const int b = s->stage_next;
+  s->stage_next ^= 1;
+  cudaError_t e = s->stage_done[b] ? cudaEventSynchronize(s->stage_done[b])
+                                   : cudaEventCreateWithFlags(&s->stage_done[b], cudaEventDisableTiming);
+  if (e != cudaSuccess) return e;
+  if (s->h_stage_cap[b] < total) {
+    if (s->h_stage[b]) cudaFreeHost(s->h_stage[b]);
+    s->h_stage[b] = nullptr;
+    s->h_stage_cap[b] = 0;
+    e = cudaHostAlloc(reinterpret_cast<void**>(&s->h_stage[b]), total, cudaHostAllocDefault);
+    if (e != cudaSuccess) return e;
+    s->h_stage_cap[b] = total;
+  }
+  *h = s->h_stage[b];
+  *slot = b;
+  return cudaSuccess;
+}
+static cudaError_t stage_send(ctgpu_scanner* s, int slot, size_t total, cudaStream_t st) {
+  cudaError_t e = ensure_device(s->d_stage, s->d_stage_cap, total);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->d_stage, s->h_stage[slot], total, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaEventRecord(s->stage_done[slot], st);
+  return e;
+}
+static size_t up16(size_t x) { return (x + 15) & ~(size_t)15; }
+// the scanner's current views' ray records (and parallel directions) into a
+// staging buffer at h (directions at h + oD)
+static void stage_ray_views(ctgpu_scanner* s, int nViews, unsigned char* h, size_t oD) {
+  s->h_rv.resize(nViews);
+  s->h_dirs.resize(s->geometry == kParallel ? (size_t)nViews * s->nSample : 0);
+  fill_ray_views(s, nViews, s->h_rv.data(), s->h_dirs.data());
+  std::memcpy(h, s->h_rv.data(), sizeof(RayView) * nViews);
+  if (!s->h_dirs.empty()) std::memcpy(h + oD, s->h_dirs.data(), sizeof(float2) * s->h_dirs.size());
+}
+
 extern "C" {
 
 int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int startView,
@@ -676,7 +723,16 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
     return ok();
   }
   CUDA_TRY(const_cast<ctgpu_phantom*>(p)->upload(st));
-  CUDA_TRY(upload_ray_views(s, nViews, st));
+  CUDA_TRY(ensure_arc_table(s));
+  // one staging copy: [ray records][parallel directions]
+  const bool par = s->geometry == kParallel;
+  const size_t oD = up16(sizeof(RayView) * nViews);
+  const size_t total = oD + (par ? sizeof(float2) * nViews * s->nSample : 0);
+  unsigned char* h = nullptr;
+  int slot = 0;
+  CUDA_TRY(stage_host(s, total, &h, &slot));
+  stage_ray_views(s, nViews, h, oD);
+  CUDA_TRY(stage_send(s, slot, total, st));
   RaysumLaunch L{};
   L.geometry = s->geometry;
   L.nDet = s->nDet;
@@ -689,8 +745,8 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
   L.angularDetLen = s->angularDetLen;
   L.angularDetInc = s->angularDetInc;
   L.elems = p->d_elems;
-  L.views = s->d_views;
-  L.sdirs = s->d_sdirs;
+  L.views = reinterpret_cast<const RayView*>(s->d_stage);
+  L.sdirs = par ? reinterpret_cast<const float2*>(s->d_stage + oD) : nullptr;
   L.arc = s->d_arc;
   L.sino = d_sino;
   L.status = status_pointer();
@@ -725,32 +781,20 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   if (h_angles)
     for (int v = 0; v < s->nView; v++) h_angles[v] = s->views[v].angle;
   CUDA_TRY(ensure_arc_table(s));
-  // one staging buffer: [ray records][parallel directions][elements][offsets]
+  // one staging copy: [ray records][parallel directions][elements][offsets]
   const int nv = s->nView;
   const bool par = s->geometry == kParallel;
-  auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
   const size_t oD = up16(sizeof(RayView) * nv);
   const size_t oE = up16(oD + (par ? sizeof(float2) * nv * s->nSample : 0));
   const size_t oO = up16(oE + sizeof(PElem) * all.size());
   const size_t total = oO + sizeof(int) * offs.size();
-  const int b = s->stage_next;
-  s->stage_next ^= 1;
-  if (s->stage_done[b]) CUDA_TRY(cudaEventSynchronize(s->stage_done[b]));   // its last copy
-  else CUDA_TRY(cudaEventCreateWithFlags(&s->stage_done[b], cudaEventDisableTiming));
-  if (s->h_stage_cap[b] < total) {
-    if (s->h_stage[b]) cudaFreeHost(s->h_stage[b]);
-    s->h_stage[b] = nullptr;
-    s->h_stage_cap[b] = 0;
-    CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&s->h_stage[b]), total, cudaHostAllocDefault));
-    s->h_stage_cap[b] = total;
-  }
-  unsigned char* h = s->h_stage[b];
-  fill_ray_views(s, nv, reinterpret_cast<RayView*>(h), reinterpret_cast<float2*>(h + oD));
+  unsigned char* h = nullptr;
+  int slot = 0;
+  CUDA_TRY(stage_host(s, total, &h, &slot));
+  stage_ray_views(s, nv, h, oD);
   if (!all.empty()) std::memcpy(h + oE, all.data(), sizeof(PElem) * all.size());
   std::memcpy(h + oO, offs.data(), sizeof(int) * offs.size());
-  CUDA_TRY(ensure_device(s->d_stage, s->d_stage_cap, total));
-  CUDA_TRY(cudaMemcpyAsync(s->d_stage, h, total, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaEventRecord(s->stage_done[b], st));
+  CUDA_TRY(stage_send(s, slot, total, st));
   RaysumLaunch L{};
   L.geometry = s->geometry;
   L.nDet = s->nDet;
@@ -811,6 +855,8 @@ int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ell, in
   CUDA_TRY(cudaMemcpyAsync(s->d_zc, zc.data(), sizeof(double2) * zc.size(),
                            cudaMemcpyHostToDevice, st));
   CUDA_TRY(launch_ellipsoid_sections(s->d_belems, s->d_zc, n, s->nView, z0, dz, s->d_velems, st));
+  // the ray records after the cross-section launch, which runs meanwhile
+  // (thousands of views: this call is bound by the host's per-view work)
   CUDA_TRY(upload_ray_views(s, s->nView, st));
   RaysumLaunch L{};
   L.geometry = s->geometry;
