@@ -494,6 +494,58 @@ def fourier_recon(args, torch, cg, device, sinos, g, angles, B):
                              "(radix-2 FFTs)"}}
 
 
+def batch_vs_plan(args):
+    """The cost of the uneven-batch path's generality: N identical problems of
+    the main workload's shape (equiangular 733 x 720 -> 512 x 512, cubic,
+    abs_hamming FFT zero-pad 2) as one ctgpu_batch and through one plan's
+    ctgpu_recon_run_batch, each timed with CUDA events over `steps` runs.
+    Prints one JSON line; nothing else runs."""
+    import torch
+    import ctsim_gb300 as cg
+    from ctsim_gb300 import device, phantoms
+    torch.cuda.set_device(0)
+    n = args.batch_vs_plan
+    probs = []
+    for i in range(n):
+        ph = phantoms.make_phantom(phantoms.random_ellipses(seed=i, n=12))
+        sc = cg.Scanner(ph, "equiangular", N_DET, N_VIEW)
+        sino = device.alloc_sinogram(N_VIEW, N_DET)
+        ang = device.raysums(sc, ph, sino)
+        probs.append(dict(geometry=sc.geometry(), nx=NX, ny=NX, sino=sino, angles=ang,
+                          image=torch.zeros((NX, NX), device="cuda"),
+                          filter_name="abs_hamming", filter_param=0.54, filter_method="fft",
+                          zeropad=2, interp="cubic", backproj="table"))
+    batch = device.BatchPlan(probs, autotune=False, graph=False)
+    plan = device.ReconPlan(probs[0]["geometry"], NX, NX, "abs_hamming", 0.54, "fft", 2,
+                            "direct", "cubic", 1, "table")
+    sinos = torch.stack([q["sino"] for q in probs])
+    images = torch.zeros((n, NX, NX), device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        torch.cuda.synchronize()
+        cg.sync()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        cg.sync()
+        return a.elapsed_time(b) / args.steps
+
+    batch_ms = timed(batch.run)
+    plan_ms = timed(lambda: plan.run_batch(sinos, probs[0]["angles"], images))
+    pv = n * PV_PER_SLICE
+    print(json.dumps({"metric": METRIC, "unit": UNIT, "problems": n, "config": CONFIG_NAME,
+                      "batch": {"value": pv / batch_ms * 1e3, "ms": batch_ms,
+                                "shape": batch.shape()},
+                      "plan_batch": {"value": pv / plan_ms * 1e3, "ms": plan_ms}}))
+    return 0
+
+
 def run_gpu(args):
     import torch
     import ctsim_gb300 as cg
@@ -704,9 +756,14 @@ def main():
                     help="problems of the uneven batch measured after the main workload (0: skip)")
     ap.add_argument("--ref-views", type=int, default=None,
                     help="views per CPU sample slice (default: all 720)")
+    ap.add_argument("--batch-vs-plan", type=int, default=0,
+                    help="only compare N identical problems as one ctgpu_batch and through "
+                         "one plan, then exit (0: the normal run)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.batch_vs_plan > 0:
+        return batch_vs_plan(args)
     return run_gpu(args)
 
 
