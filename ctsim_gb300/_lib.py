@@ -106,6 +106,7 @@ SIGNATURES = {
     "ctgpu_recon_run_batch": ([_p, _i, _p, _i, C.c_longlong, _p, _p, C.c_longlong, _i, _p], _i),
     "ctgpu_recon_run_batch_host": ([_p, _i, _p, _p, _p, _i], _i),
     "ctgpu_recon_host_chunks": ([_p, _i, _p, _i], _i),
+    "ctgpu_recon_set_host_chunks": ([_p, _p, _i], _i),
     "ctgpu_recon_backproject_batch": ([_p, _i, _p, _i, C.c_longlong, _p, _i, _p, C.c_longlong,
                                        _i, _p], _i),
     "ctgpu_recon_project": ([_p, _p, _p, _i, _p, _i, _f, _p], _i),

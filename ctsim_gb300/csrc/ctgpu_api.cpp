@@ -310,24 +310,33 @@ struct ctgpu_recon {
   size_t d_sino_cap = 0;
   float* d_image = nullptr;
   size_t d_image_cap = 0;
-  // run_batch_host: two chunk buffers each, copy / compute streams and events
+  // run_batch_host: two chunk buffers each, copy / compute streams and events;
+  // chunks of odd index run on s_comp2 with their own filtered rows and
+  // set-up scratch, so that consecutive chunks overlap on the device
   float* d_bsino = nullptr;
   size_t d_bsino_cap = 0;
   float* d_bimage = nullptr;
   size_t d_bimage_cap = 0;
-  cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
+  float* d_filtered2 = nullptr;
+  size_t d_filtered2_cap = 0;
+  unsigned char* d_scratch2 = nullptr;
+  size_t d_scratch2_cap = 0;
+  cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr, s_comp2 = nullptr;
   cudaEvent_t ev[6] = {};   // in_done[2], comp_done[2], out_done[2]
   double* h_angles_pinned = nullptr;   // page-locked copy of the view angles
   size_t h_angles_cap = 0;
+  std::vector<int> hostChunks;         // chunk sizes set by the caller (empty: planned)
+  mutable std::vector<int> plannedChunks;   // the last plan, for plannedFor slices on plannedDev
+  mutable int plannedFor = 0, plannedDev = -1;
   ~ctgpu_recon() {
     if (h_angles_pinned) cudaFreeHost(h_angles_pinned);
     for (void* p : {(void*)d_spec, (void*)d_weights, (void*)d_filtered, (void*)d_angles,
                     (void*)d_views, (void*)d_scratch, (void*)d_sino, (void*)d_image,
-                    (void*)d_bsino, (void*)d_bimage})
+                    (void*)d_bsino, (void*)d_bimage, (void*)d_filtered2, (void*)d_scratch2})
       if (p) cudaFree(p);
     for (cudaEvent_t e : ev)
       if (e) cudaEventDestroy(e);
-    for (cudaStream_t s : {s_in, s_comp, s_out})
+    for (cudaStream_t s : {s_in, s_comp, s_out, s_comp2})
       if (s) cudaStreamDestroy(s);
   }
 };
@@ -1171,14 +1180,16 @@ static BackprojLaunch make_launch(const ctgpu_recon* r, int nViews, int pitch,
 // Backprojection of nViews filtered rows; outScale multiplies this launch's sum.
 // reuseScratch: the scratch whose (tile, view) records an earlier launch on
 // stream st built for the same view angles (table family), or null;
-// anglesOnDevice: r->d_angles already holds h_angles, ordered before st's work
+// anglesOnDevice: r->d_angles already holds h_angles, ordered before st's work;
+// extScratch: set-up scratch the caller sized (null: the plan's own)
 static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int pitch,
                                     const double* h_angles, int nViews, float* d_image,
                                     int accumulate, float outScale, cudaStream_t st,
                                     int nBatch = 1, size_t filtStride = 0,
                                     size_t imageStride = 0,
                                     const unsigned char* reuseScratch = nullptr,
-                                    bool anglesOnDevice = false) {
+                                    bool anglesOnDevice = false,
+                                    unsigned char* extScratch = nullptr) {
   if (nViews <= 0) {
     if (!accumulate)
       for (int b = 0; b < nBatch; b++)
@@ -1188,7 +1199,8 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
   if (nBatch > 1 && r->bproj == kDiff) {
     for (int b = 0; b < nBatch; b++) {
       int rc = recon_backproject_scaled(r, d_filtered + b * filtStride, pitch, h_angles, nViews,
-                                        d_image + b * imageStride, accumulate, outScale, st);
+                                        d_image + b * imageStride, accumulate, outScale, st, 1, 0,
+                                        0, nullptr, anglesOnDevice, extScratch);
       if (rc) return rc;
     }
     return ok();
@@ -1225,12 +1237,17 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
   BackprojLaunch L = make_launch(r, nViews, pitch, r->d_angles, d_filtered, d_image, accumulate,
                                  outScale, nBatch, filtStride, imageStride);
   size_t sb = backproject_scratch_bytes(L);
-  const size_t capBefore = r->d_scratch_cap;
-  if (sb) CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
-  // a reallocated scratch (even at the same address) holds no records
-  L.reuseRecords = reuseScratch && reuseScratch == r->d_scratch && r->d_scratch_cap == capBefore &&
-                   r->bproj != kDiff && r->bproj != kIDiff;
-  cudaError_t e = launch_backproject_views(L, views, r->d_scratch, st);
+  unsigned char* scratch = extScratch;
+  bool stable = true;
+  if (!scratch) {
+    const size_t capBefore = r->d_scratch_cap;
+    if (sb) CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
+    scratch = r->d_scratch;
+    stable = r->d_scratch_cap == capBefore;   // a reallocated scratch holds no records
+  }
+  L.reuseRecords = reuseScratch && reuseScratch == scratch && stable && r->bproj != kDiff &&
+                   r->bproj != kIDiff;
+  cudaError_t e = launch_backproject_views(L, views, scratch, st);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "image pixels behind the fan-beam source");
   CUDA_TRY(e);
@@ -1297,10 +1314,16 @@ int ctgpu_recon_run_host(ctgpu_recon* r, const float* h_sino, const double* h_an
   return ctgpu_sync(nullptr);
 }
 
+// filtered rows and set-up scratch of one host-batch chunk, sized by the caller
+struct ChunkBufs {
+  float* filtered;
+  unsigned char* scratch;
+};
 static int recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int sinoPitch,
                            long long sinoSliceStride, const double* h_angles, float* d_images,
                            long long imageSliceStride, int flags, cudaStream_t st,
-                           const unsigned char* reuseScratch, bool anglesOnDevice);
+                           const unsigned char* reuseScratch, bool anglesOnDevice,
+                           const ChunkBufs* bufs = nullptr);
 
 int ctgpu_recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int sinoPitch,
                           long long sinoSliceStride, const double* h_angles, float* d_images,
@@ -1312,7 +1335,8 @@ int ctgpu_recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int 
 static int recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int sinoPitch,
                            long long sinoSliceStride, const double* h_angles, float* d_images,
                            long long imageSliceStride, int flags, cudaStream_t st,
-                           const unsigned char* reuseScratch, bool anglesOnDevice) {
+                           const unsigned char* reuseScratch, bool anglesOnDevice,
+                           const ChunkBufs* bufs) {
   if (!r || !d_sinos || !h_angles || !d_images) return fail(CTGPU_ERR_INVALID, "null argument");
   if (nBatch < 1) return fail(CTGPU_ERR_INVALID, "batch size must be >= 1");
   const int nView = r->g.n_view;
@@ -1321,58 +1345,90 @@ static int recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int
     return fail(CTGPU_ERR_INVALID, "pitch / slice strides too small");
   if (flags & CTGPU_RUN_ACCUMULATE) return fail(CTGPU_ERR_UNSUPPORTED, "batched runs overwrite their images");
   size_t fStride = (size_t)nView * r->pitch;
-  CUDA_TRY(ensure_device(r->d_filtered, r->d_filtered_cap, fStride * nBatch));
+  float* filtered = bufs ? bufs->filtered : nullptr;
+  if (!filtered) {
+    CUDA_TRY(ensure_device(r->d_filtered, r->d_filtered_cap, fStride * nBatch));
+    filtered = r->d_filtered;
+  }
   int rc = recon_filter_batch(r, d_sinos, sinoPitch, (size_t)sinoSliceStride, nView,
-                              r->d_filtered, r->pitch, fStride, nBatch, st);
+                              filtered, r->pitch, fStride, nBatch, st);
   if (rc) return rc;
   float scale = raw_scale(r);
   bool post = (flags & CTGPU_RUN_POSTPROCESS) != 0;
   if (post && r->bproj != kTrig) scale = (float)(scale * r->rotScale);
-  return recon_backproject_scaled(r, r->d_filtered, r->pitch, h_angles, nView, d_images, 0, scale,
+  return recon_backproject_scaled(r, filtered, r->pitch, h_angles, nView, d_images, 0, scale,
                                   st, nBatch, fStride, (size_t)imageSliceStride, reuseScratch,
-                                  anglesOnDevice);
+                                  anglesOnDevice, bufs ? bufs->scratch : nullptr);
 }
 
-// Chunk sizes of a host-buffer batch.  A backprojection launch of s slices
-// runs ceil(s * tiles / resident) waves of blocks: a wave is paid whole
-// however few of its blocks have work.  The first chunk's input copy and the
-// last chunk's output copy are not hidden behind compute; every other copy
-// is.  The sizes minimise, by dynamic programming over the slices, the waves
-// plus the two exposed copies plus a fixed cost per chunk, all in
-// milliseconds from rough GB300 rates (1.1e12 pixel-view updates/s, 200 GB/s
-// host to device, 180 GB/s back, 20 us between chunks).
+// Chunk sizes of a host-buffer batch.  Consecutive chunks run on two compute
+// streams, so the device stays busy across chunk boundaries: a chunk costs its
+// blocks' share of the resident slots (s * tiles / resident waves) plus a
+// small fixed cost.  Exposed are the first chunk's input copy, the last
+// chunk's output copy, a wait wherever a chunk's input copy outlasts the
+// previous chunk's compute, and the second-to-last chunk's output copy where it
+// outlasts the last chunk's compute.  A dynamic program over (slices covered,
+// last chunk size) minimises the sum, in milliseconds from rough GB300 rates
+// (1.1e12 pixel-view updates/s, 200 GB/s host to device, 180 GB/s back,
+// 10 us per chunk).  For 64 slices of 512^2 it picks 1 + 17 + 44 + 2.
 static std::vector<int> plan_chunks(int nBatch, int maxChunk, long long tilesPerSlice,
                                     long long resident, double waveMs, double inMs, double outMs) {
-  const double chunkMs = 0.02;
-  auto body = [&](int sz) {
-    const long long ctas = tilesPerSlice * sz;
-    return (double)((ctas + resident - 1) / resident) * waveMs + chunkMs;
-  };
+  const int S = std::min(maxChunk, nBatch);
+  auto comp = [&](int sz) { return (double)(tilesPerSlice * sz) / resident * waveMs + 0.01; };
   const double inf = 1e300;
-  std::vector<double> best(nBatch + 1, inf);
-  std::vector<int> last(nBatch + 1, 0);
-  best[0] = 0;
-  for (int i = 1; i <= nBatch; i++)
-    for (int sz = 1; sz <= maxChunk && sz <= i; sz++) {
-      double c = best[i - sz] + body(sz) + (i == sz ? inMs * sz : 0.0) + (i == nBatch ? outMs * sz : 0.0);
-      if (c < best[i]) {
-        best[i] = c;
-        last[i] = sz;
+  // f[i * (S + 1) + s]: the first i slices covered, the last chunk of size s
+  std::vector<double> f((size_t)(nBatch + 1) * (S + 1), inf);
+  std::vector<int> prev((size_t)(nBatch + 1) * (S + 1), 0);
+  auto at = [&](int i, int sz) { return (size_t)i * (S + 1) + sz; };
+  for (int sz = 1; sz <= S; sz++) f[at(sz, sz)] = inMs * sz + comp(sz);
+  for (int i = 1; i < nBatch; i++)
+    for (int sz = 1; sz <= std::min(S, i); sz++) {
+      const double base = f[at(i, sz)];
+      if (base >= inf) continue;
+      for (int s2 = 1; s2 <= std::min(S, nBatch - i); s2++) {
+        const double c = base + comp(s2) + std::max(0.0, inMs * s2 - comp(sz));
+        if (c < f[at(i + s2, s2)]) {
+          f[at(i + s2, s2)] = c;
+          prev[at(i + s2, s2)] = sz;
+        }
       }
     }
+  double best = inf;
+  int last = 1;
+  for (int sz = 1; sz <= S; sz++) {
+    if (f[at(nBatch, sz)] >= inf) continue;
+    const int p = prev[at(nBatch, sz)];
+    const double c = f[at(nBatch, sz)] + outMs * sz + (p ? std::max(0.0, outMs * p - comp(sz)) : 0.0);
+    if (c < best) {
+      best = c;
+      last = sz;
+    }
+  }
   std::vector<int> sizes;
-  for (int i = nBatch; i > 0; i -= last[i]) sizes.push_back(last[i]);
+  for (int i = nBatch, sz = last; i > 0;) {
+    sizes.push_back(sz);
+    const int p = prev[at(i, sz)];
+    i -= sz;
+    sz = p;
+  }
   std::reverse(sizes.begin(), sizes.end());
   return sizes;
 }
 
 // the chunks of a host-buffer batch of nBatch slices on the current device
+// (the plan's last answer when asked again)
 static cudaError_t host_chunk_sizes(const ctgpu_recon* r, int nBatch, std::vector<int>* sizes) {
+  int dev = 0;
+  cudaError_t e0 = cudaGetDevice(&dev);
+  if (e0 != cudaSuccess) return e0;
+  if (r->plannedFor == nBatch && r->plannedDev == dev) {
+    *sizes = r->plannedChunks;
+    return cudaSuccess;
+  }
   const int nView = r->g.n_view;
   const size_t sStride = (size_t)nView * r->g.n_det, iStride = (size_t)r->nx * r->ny;
-  int sms = 0, dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int sms = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
   // at most 64 slices and 1 GiB of staging per chunk buffer
   const size_t sliceBytes = sizeof(float) * (sStride + iStride);
@@ -1383,14 +1439,38 @@ static cudaError_t host_chunk_sizes(const ctgpu_recon* r, int nBatch, std::vecto
   const double waveMs = (double)resident * kBackprojTile * kBackprojTile * nView / 1.1e9;
   *sizes = plan_chunks(nBatch, maxChunk, tilesPerSlice, resident, waveMs,
                        sizeof(float) * sStride / 2e8, sizeof(float) * iStride / 1.8e8);
+  r->plannedChunks = *sizes;
+  r->plannedFor = nBatch;
+  r->plannedDev = dev;
   return cudaSuccess;
+}
+
+// the caller's chunk sizes, repeated from the start until n_batch slices are
+// covered (the last one cut short), or the planned ones
+static cudaError_t host_chunks_for(const ctgpu_recon* r, int nBatch, std::vector<int>* sizes) {
+  if (r->hostChunks.empty()) return host_chunk_sizes(r, nBatch, sizes);
+  sizes->clear();
+  for (int left = nBatch, k = 0; left > 0; k++) {
+    const int n = std::min(left, r->hostChunks[k % r->hostChunks.size()]);
+    sizes->push_back(n);
+    left -= n;
+  }
+  return cudaSuccess;
+}
+
+int ctgpu_recon_set_host_chunks(ctgpu_recon* r, const int* sizes, int n) {
+  if (!r || (n > 0 && !sizes) || n < 0) return fail(CTGPU_ERR_INVALID, "null argument");
+  for (int i = 0; i < n; i++)
+    if (sizes[i] < 1) return fail(CTGPU_ERR_INVALID, "chunk sizes must be >= 1");
+  r->hostChunks.assign(sizes, sizes + n);
+  return ok();
 }
 
 int ctgpu_recon_host_chunks(const ctgpu_recon* r, int nBatch, int* sizes, int maxSizes) {
   if (!r || (!sizes && maxSizes > 0)) return fail(CTGPU_ERR_INVALID, "null argument");
   if (nBatch < 1) return fail(CTGPU_ERR_INVALID, "batch size must be >= 1");
   std::vector<int> v;
-  CUDA_TRY(host_chunk_sizes(r, nBatch, &v));
+  CUDA_TRY(host_chunks_for(r, nBatch, &v));
   for (int i = 0; i < (int)v.size() && i < maxSizes; i++) sizes[i] = v[i];
   return (int)v.size();
 }
@@ -1405,7 +1485,7 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
   // the filter reads them at pitch n_det and writes the aligned filtered rows
   const size_t sStride = (size_t)nView * nDet, iStride = (size_t)r->nx * r->ny;
   std::vector<int> sizes;
-  CUDA_TRY(host_chunk_sizes(r, nBatch, &sizes));
+  CUDA_TRY(host_chunks_for(r, nBatch, &sizes));
   std::vector<int> first;
   int chunk = 0;
   for (size_t c = 0, at = 0; c < sizes.size(); at += sizes[c], c++) {
@@ -1422,7 +1502,7 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
                            sizeof(double) * (nView ? nView : 1), cudaHostAllocDefault));
     r->h_angles_cap = nView;
   }
-  for (cudaStream_t* s : {&r->s_in, &r->s_comp, &r->s_out})
+  for (cudaStream_t* s : {&r->s_in, &r->s_comp, &r->s_out, &r->s_comp2})
     if (!*s) CUDA_TRY(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking));
   for (cudaEvent_t& e : r->ev)
     if (!e) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1438,16 +1518,24 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
   cudaEvent_t* compDone = r->ev + 2;
   cudaEvent_t* outDone = r->ev + 4;
   const int nChunks = (int)sizes.size();
-  const unsigned char* recScratch = nullptr;
+  // two sets of filtered rows and set-up scratch, one per compute stream,
+  // each sized for the largest chunk up front: no buffer is reallocated (a
+  // synchronising free) between chunks, and each set's records stay put
+  ChunkBufs bufs[2];
+  cudaStream_t comp[2] = {r->s_comp, r->s_comp2};
+  const unsigned char* recScratch[2] = {nullptr, nullptr};
   {
-    // filtered rows and scratch for the largest chunk up front: no buffer is
-    // reallocated (a synchronising free) between chunks, and the records stay put
     const size_t fStride = (size_t)nView * r->pitch;
+    const int sets = nChunks > 1 ? 2 : 1;
     CUDA_TRY(ensure_device(r->d_filtered, r->d_filtered_cap, fStride * chunk));
+    if (sets > 1) CUDA_TRY(ensure_device(r->d_filtered2, r->d_filtered2_cap, fStride * chunk));
     BackprojLaunch L = make_launch(r, nView, r->pitch, nullptr, nullptr, nullptr, 0, 1.f, chunk,
                                    fStride, iStride);
     const size_t sb = backproject_scratch_bytes(L);
-    if (sb) CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
+    CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb ? sb : 1));
+    if (sets > 1) CUDA_TRY(ensure_device(r->d_scratch2, r->d_scratch2_cap, sb ? sb : 1));
+    bufs[0] = ChunkBufs{r->d_filtered, r->d_scratch};
+    bufs[1] = ChunkBufs{r->d_filtered2, r->d_scratch2};
   }
   // image copy of chunk c, issued one iteration late so that a pageable
   // destination (whose copy blocks the host) does not hold back the next
@@ -1460,6 +1548,8 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
     CUDA_TRY(cudaEventRecord(outDone[b], r->s_out));
     return CTGPU_OK;
   };
+  // chunk c runs on compute stream c & 1 with buffer set c & 1: the next
+  // chunk's filter and backprojection start in this one's tail
   for (int c = 0; c < nChunks; c++) {
     const int b = c & 1, n = sizes[c];
     float* dS = r->d_bsino + b * chunk * sStride;
@@ -1468,21 +1558,23 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
     CUDA_TRY(cudaMemcpyAsync(dS, h_sinos + (size_t)first[c] * sStride, sizeof(float) * sStride * n,
                              cudaMemcpyHostToDevice, r->s_in));
     CUDA_TRY(cudaEventRecord(inDone[b], r->s_in));
-    CUDA_TRY(cudaStreamWaitEvent(r->s_comp, inDone[b], 0));
-    if (c >= 2) CUDA_TRY(cudaStreamWaitEvent(r->s_comp, outDone[b], 0));   // image b copied out
-    // every chunk has the same view angles: the first builds the (tile, view)
-    // records, the later ones on the same stream use them
+    CUDA_TRY(cudaStreamWaitEvent(comp[b], inDone[b], 0));
+    if (c >= 2) CUDA_TRY(cudaStreamWaitEvent(comp[b], outDone[b], 0));   // image b copied out
+    // every chunk has the same view angles: the first chunk of each set
+    // builds its (tile, view) records, the set's later chunks (same stream)
+    // use them
     int rc = recon_run_batch(r, n, dS, nDet, (long long)sStride, r->h_angles_pinned, dI,
-                             (long long)iStride, flags & CTGPU_RUN_POSTPROCESS, r->s_comp,
-                             c > 0 ? recScratch : nullptr, true);
+                             (long long)iStride, flags & CTGPU_RUN_POSTPROCESS, comp[b],
+                             recScratch[b], true, &bufs[b]);
     if (rc) return rc;
-    if (c == 0) recScratch = r->d_scratch;
-    CUDA_TRY(cudaEventRecord(compDone[b], r->s_comp));
+    recScratch[b] = bufs[b].scratch;
+    CUDA_TRY(cudaEventRecord(compDone[b], comp[b]));
     if (c >= 1 && (rc = copy_out(c - 1))) return rc;
   }
   int rc = copy_out(nChunks - 1);
   if (rc) return rc;
-  CUDA_TRY(cudaStreamSynchronize(r->s_out));
+  CUDA_TRY(cudaStreamSynchronize(r->s_out));   // after every chunk's compute
+  CUDA_TRY(cudaStreamSynchronize(r->s_comp2));
   return ctgpu_sync(r->s_comp);
 }
 

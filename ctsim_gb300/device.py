@@ -191,6 +191,11 @@ class ReconPlan:
             n = lib().ctgpu_recon_host_chunks(self._h, int(n_batch), C.cast(sizes, C.c_void_p), n)
         return list(sizes[:n])
 
+    def set_host_chunks(self, sizes=()):
+        """fix run_batch_host's chunk sizes (used in turn); () restores the planned ones"""
+        arr = (C.c_int * max(len(sizes), 1))(*[int(x) for x in sizes])
+        check(lib().ctgpu_recon_set_host_chunks(self._h, C.cast(arr, C.c_void_p), len(sizes)))
+
     def project(self, image, angles, out, scale=1.0, stream=None):
         ang = np.ascontiguousarray(angles, np.float64)
         check(lib().ctgpu_recon_project(self._h, _ptr(image), ang.ctypes.data_as(C.c_void_p),

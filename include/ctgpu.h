@@ -214,12 +214,13 @@ int ctgpu_recon_run_batch(ctgpu_recon* r, int n_batch, const float* d_sinos, int
                           void* stream);
 /* ctgpu_recon_run_batch with host buffers: h_sinos n_batch sinograms
  * [n_view][n_det] back to back, h_images n_batch images [nx][ny] back to back.
- * Slices move in chunks through two device buffers, so the copy of one chunk
- * overlaps the reconstruction of the previous one (page-locked host buffers
- * make the copies asynchronous; pageable ones work, with less overlap).  The
- * chunk sizes (ctgpu_recon_host_chunks) keep each backprojection launch to
- * whole waves of blocks on this GPU and the first and last chunks' copies
- * short; the chunks share one set of (tile, view) records.  Synchronous:
+ * Slices move in chunks through two sets of device buffers on two compute
+ * streams, so the copies of one chunk overlap the reconstruction of its
+ * neighbours and consecutive chunks overlap on the device (page-locked host
+ * buffers make the copies asynchronous; pageable ones work, with less
+ * overlap).  The chunk sizes (ctgpu_recon_host_chunks) keep the first and last
+ * chunks' copies short; each buffer set builds its (tile, view) records once
+ * per call.  Synchronous:
  * returns when h_images is written.  No reference counterpart (CTSim
  * reconstructs one slice per Reconstructor). */
 int ctgpu_recon_run_batch_host(ctgpu_recon* r, int n_batch, const float* h_sinos,
@@ -228,6 +229,10 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int n_batch, const float* h_sinos
  * current device: the first min(count, max_sizes) go to sizes; returns the
  * number of chunks (>= 1), or a negative error.  No reference counterpart. */
 int ctgpu_recon_host_chunks(const ctgpu_recon* r, int n_batch, int* sizes, int max_sizes);
+/* Fixes ctgpu_recon_run_batch_host's chunk sizes: sizes[0..n) in turn from the
+ * first slice (repeated, the last chunk cut short); n = 0 restores the planned
+ * sizes.  No reference counterpart. */
+int ctgpu_recon_set_host_chunks(ctgpu_recon* r, const int* sizes, int n);
 /* Backprojection of n_batch filtered sinograms (same geometry and angles) in
  * one launch; flags: CTGPU_RUN_POSTPROCESS folds PostProcessing in. */
 int ctgpu_recon_backproject_batch(ctgpu_recon* r, int n_batch, const float* d_filtered,

@@ -292,18 +292,24 @@ def test_batch_host_equals_device_batch(gpu, pinned):
         assert rel_l2(res[b], r[b]) < 1e-7, b
 
 
-def test_batch_host_chunks_share_records(gpu):
+@pytest.mark.parametrize("geo,interp,backproj", [("equiangular", "cubic", "table"),
+                                                  ("parallel", "linear", "trig"),
+                                                  ("parallel", "linear", "diff"),
+                                                  ("parallel", "nearest", "idiff")])
+def test_batch_host_chunks_share_records(gpu, geo, interp, backproj):
     """A host batch split into chunks of different sizes, a later one larger
-    than the first (buffers sized for the largest up front, the first chunk's
-    (tile, view) records used by the rest): the device batch's images, bit
-    for bit.  The chunk plan covers every slice once for any batch size."""
+    than the first, consecutive chunks on two compute streams with their own
+    buffers (sized for the largest chunk up front; each set's first chunk
+    builds the (tile, view) records its later chunks use): the device batch's
+    images, bit for bit.  The chunk plan covers every slice once for any
+    batch size."""
     torch, cg, device = gpu
     from ctsim_gb300 import phantoms
     nd, nv, n = 367, 360, 256
     ph0 = phantoms.make_phantom(phantoms.random_ellipses(seed=900, n=5))
-    sc = cg.Scanner(ph0, "equiangular", nd, nv)
+    sc = cg.Scanner(ph0, geo, nd, nv)
     g = sc.geometry()
-    plan = device.ReconPlan(g, n, n, "abs_hamming", 0.54, "fft", 2, "direct", "cubic", 1, "table")
+    plan = device.ReconPlan(g, n, n, "abs_hamming", 0.54, "fft", 2, "direct", interp, 1, backproj)
     for b in (1, 2, 7, 33, 100, 500):
         sizes = plan.host_chunks(b)
         assert sum(sizes) == b and min(sizes) >= 1, (b, sizes)
@@ -323,6 +329,16 @@ def test_batch_host_chunks_share_records(gpu):
         out.zero_()
         plan.run_batch_host(host, angs, out)
         assert torch.equal(out, ref.cpu()), plan.host_chunks(B)
+    # chunk sizes fixed by the caller: used in turn, the last one cut short
+    planned = plan.host_chunks(B)
+    plan.set_host_chunks([3, 5])
+    fixed = plan.host_chunks(B)
+    assert sum(fixed) == B and fixed[:4] == [3, 5, 3, 5], fixed
+    out.zero_()
+    plan.run_batch_host(host, angs, out)
+    assert torch.equal(out, ref.cpu()), fixed
+    plan.set_host_chunks()
+    assert plan.host_chunks(B) == planned
 
 
 @pytest.mark.parametrize("geo,nray", [("parallel", 2), ("equiangular", 1), ("equilinear", 3)])
