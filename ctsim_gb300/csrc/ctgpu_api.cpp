@@ -293,6 +293,7 @@ struct ctgpu_recon {
   ctgpu_geometry g;
   int nx, ny, interp, bproj, interpFactor;
   int iDetCenter, pitch;
+  int sms = 0;   // SMs of the device (single-slice view groups), queried once
   double xMin, xMax, yMin, yMax, xInc, yInc, rotScale, startR, startPhi;
   FilterDesign fd;
   int fftN = 0;
@@ -1181,7 +1182,10 @@ static BackprojLaunch make_launch(const ctgpu_recon* r, int nViews, int pitch,
 // reuseScratch: the scratch whose (tile, view) records an earlier launch on
 // stream st built for the same view angles (table family), or null;
 // anglesOnDevice: r->d_angles already holds h_angles, ordered before st's work;
-// extScratch: set-up scratch the caller sized (null: the plan's own)
+// extScratch: set-up scratch the caller sized (null: the plan's own);
+// splitViews: a one-slice launch of few tiles may split its views into groups
+// (table family; the single-slice entry points, not the batched ones, whose
+// images stay bit-identical to one another)
 static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int pitch,
                                     const double* h_angles, int nViews, float* d_image,
                                     int accumulate, float outScale, cudaStream_t st,
@@ -1189,7 +1193,8 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
                                     size_t imageStride = 0,
                                     const unsigned char* reuseScratch = nullptr,
                                     bool anglesOnDevice = false,
-                                    unsigned char* extScratch = nullptr) {
+                                    unsigned char* extScratch = nullptr,
+                                    bool splitViews = false) {
   if (nViews <= 0) {
     if (!accumulate)
       for (int b = 0; b < nBatch; b++)
@@ -1236,6 +1241,14 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
   }
   BackprojLaunch L = make_launch(r, nViews, pitch, r->d_angles, d_filtered, d_image, accumulate,
                                  outScale, nBatch, filtStride, imageStride);
+  if (splitViews && nBatch == 1) {
+    if (!r->sms) {
+      int dev = 0;
+      CUDA_TRY(cudaGetDevice(&dev));
+      CUDA_TRY(cudaDeviceGetAttribute(&r->sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    L.viewGroups = table_view_groups(L, r->sms);
+  }
   size_t sb = backproject_scratch_bytes(L);
   unsigned char* scratch = extScratch;
   bool stable = true;
@@ -1268,7 +1281,8 @@ int ctgpu_recon_backproject(ctgpu_recon* r, const float* d_filtered, int pitch,
   if (pitch < r->g.n_det || (pitch & 3)) return fail(CTGPU_ERR_INVALID, "filtered pitch must be >= nDet and a multiple of 4");
   if (((uintptr_t)d_filtered & 15) != 0) return fail(CTGPU_ERR_INVALID, "filtered rows must be 16-byte aligned");
   return recon_backproject_scaled(r, d_filtered, pitch, h_angles, nViews, d_image, accumulate,
-                                  raw_scale(r), (cudaStream_t)stream);
+                                  raw_scale(r), (cudaStream_t)stream, 1, 0, 0, nullptr, false,
+                                  nullptr, true);
 }
 
 int ctgpu_recon_postprocess(ctgpu_recon* r, float* d_image, void* stream) {
@@ -1293,7 +1307,7 @@ int ctgpu_recon_run(ctgpu_recon* r, const float* d_sino, int sinoPitch, const do
   float scale = raw_scale(r);
   if (post && !acc && r->bproj != kTrig) scale = (float)(scale * r->rotScale);   // fused PostProcessing
   rc = recon_backproject_scaled(r, r->d_filtered, r->pitch, h_angles + startView, nViews, d_image,
-                                acc ? 1 : 0, scale, st);
+                                acc ? 1 : 0, scale, st, 1, 0, 0, nullptr, false, nullptr, true);
   if (rc) return rc;
   if (post && acc) return ctgpu_recon_postprocess(r, d_image, stream);
   return ok();

@@ -122,6 +122,12 @@ struct BackprojLaunch {
   // table family: the (tile, view) records in scratch were built by an earlier
   // launch of the same plan and view angles, ordered before this one
   int reuseRecords;
+  // table family, one slice: > 1 splits its views into this many groups
+  // (grid.z), each writing a partial image that one pass then sums in group
+  // order (table_view_groups picks it); partial: the groups' images
+  // [viewGroups][nx][ny] (set by the launch, in the set-up scratch)
+  int viewGroups;
+  float* partial;
 };
 
 struct HelicalLaunch {
@@ -226,6 +232,8 @@ cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
 size_t backproject_scratch_bytes(const BackprojLaunch& L);
 // blocks of the table-family main kernel resident per SM (its occupancy target)
 int backproject_table_ctas_per_sm();
+// view groups for a one-slice table-family launch on `sms` SMs (1: no split)
+int table_view_groups(const BackprojLaunch& L, int sms);
 constexpr int kBackprojTile = 32;   // image pixels per tile side
 
 // The table-family backprojection as set-up launches plus a main launch, for

@@ -73,7 +73,8 @@ def test_batch_equals_single_problems(gpu, autotune, graph):
         for i, (q, r) in enumerate(zip(probs, refs)):
             a, b = q["image"].cpu().numpy(), r.cpu().numpy()
             assert np.isfinite(a).all(), (rep, i)
-            assert rel_l2(a, b) < 1e-7, (rep, i, q["geometry"].geometry, q["interp"], rel_l2(a, b))
+            # the single-slice run may sum its views in groups (FP32 order)
+            assert rel_l2(a, b) < 1e-6, (rep, i, q["geometry"].geometry, q["interp"], rel_l2(a, b))
     bps, cv = batch.shape()
     assert bps in (2, 3, 4) and cv in (8, 16)
 

@@ -341,6 +341,37 @@ def test_batch_host_chunks_share_records(gpu, geo, interp, backproj):
     assert plan.host_chunks(B) == planned
 
 
+@pytest.mark.parametrize("geo,n,interp", [("equiangular", 512, "cubic"), ("parallel", 256, "linear"),
+                                          ("equilinear", 128, "nearest"), ("parallel", 96, "cubic")])
+def test_single_slice_view_groups(gpu, geo, n, interp):
+    """A single slice of few tiles splits its views into groups whose partial
+    images are summed in order: the same image as the batched (unsplit)
+    launch to FP32 rounding, also when the views come in two accumulated
+    halves (reconstructView + postProcessing)."""
+    torch, cg, device = gpu
+    from ctsim_gb300 import phantoms
+    nd, nv = int(1.4 * n) | 1, 360
+    ph = phantoms.make_phantom(phantoms.random_ellipses(seed=77, n=8))
+    sc = cg.Scanner(ph, geo, nd, nv)
+    sino = device.alloc_sinogram(nv, nd)
+    ang = device.raysums(sc, ph, sino)
+    plan = device.ReconPlan(sc.geometry(), n, n, "abs_hamming", 0.54, "fft", 2, "direct", interp,
+                            1, "table")
+    one = torch.zeros((n, n), device="cuda")
+    plan.run(sino, ang, one)
+    batch = torch.zeros((2, n, n), device="cuda")
+    plan.run_batch(torch.stack([sino, sino]), ang, batch)
+    halves = torch.zeros((n, n), device="cuda")
+    plan.run(sino, ang, halves, start_view=0, n_views=nv // 2, accumulate=True, postprocess=False)
+    plan.run(sino, ang, halves, start_view=nv // 2, n_views=nv - nv // 2, accumulate=True,
+             postprocess=True)
+    cg.sync()
+    ref = batch[0].cpu().numpy()
+    assert torch.equal(batch[0], batch[1])
+    assert rel_l2(one.cpu().numpy(), ref) < 1e-6, rel_l2(one.cpu().numpy(), ref)
+    assert rel_l2(halves.cpu().numpy(), ref) < 1e-6, rel_l2(halves.cpu().numpy(), ref)
+
+
 @pytest.mark.parametrize("geo,nray", [("parallel", 2), ("equiangular", 1), ("equilinear", 3)])
 def test_raysums_batch_equals_single(gpu, geo, nray):
     """ctgpu_collect_projections_batch (all phantoms in one launch) writes the
