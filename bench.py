@@ -643,6 +643,20 @@ def run_gpu(args):
     e2e_err = float(np.linalg.norm(host_images.numpy() - dev_imgs) / np.linalg.norm(dev_imgs))
     one = plan.run_host(host_sinos[B - 1].numpy(), angles[0])
     single_err = float(np.linalg.norm(one - dev_imgs[B - 1]) / np.linalg.norm(dev_imgs[B - 1]))
+    # one slice through the single-slice entry point (the C++ Reconstructor's
+    # and pjrec's call; device-resident sinogram), CUDA events
+    one_img = torch.zeros((NX, NX), device="cuda")
+    for _ in range(max(args.warmup, 1)):
+        plan.run(sinos[0], angles[0], one_img)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for _ in range(max(args.steps, 1)):
+        plan.run(sinos[0], angles[0], one_img)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    cg.sync()
+    single_ms = s0.elapsed_time(s1) / max(args.steps, 1)
 
     batched = batched_uneven(args, torch, cg, device, phantoms, rank) \
         if args.batched_problems > 0 else None
@@ -723,6 +737,8 @@ def run_gpu(args):
                 "single_slice_run_host_rel_l2": single_err},
         # per step: one filter launch; interval rows, tile records and the
         # backprojection itself for the batch
+        "single_slice": {"ms": single_ms, "value": PV_PER_SLICE / (single_ms / 1e3), "unit": UNIT,
+                         "call": "ctgpu_recon_run (one slice, its views in groups of blocks)"},
         "gpu_launches": steps * 4,
         "batched_uneven": batched,
         "helical": helical,
