@@ -260,6 +260,10 @@ struct ctgpu_scanner {
   // step arcDelta
   double2* d_arc = nullptr;
   size_t d_arc_cap = 0;
+  // and in FP32 of the half angles, (cos, sin) of t * delta / 2: the rays'
+  // directions
+  float2* d_half = nullptr;
+  size_t d_half_cap = 0;
   int arcN = 0;
   double arcDelta = 0;
   // the ray-sum calls' per-call inputs (the views' ray records, parallel ray
@@ -280,7 +284,7 @@ struct ctgpu_scanner {
   ~ctgpu_scanner() {
     for (void* p : {(void*)d_views, (void*)d_sino, (void*)d_belems,
                     (void*)d_sdirs, (void*)d_records, (void*)d_velems, (void*)d_zc,
-                    (void*)d_arc, (void*)d_stage})
+                    (void*)d_arc, (void*)d_half, (void*)d_stage})
       if (p) cudaFree(p);
     for (int b = 0; b < 2; b++) {
       if (h_stage[b]) cudaFreeHost(h_stage[b]);
@@ -642,16 +646,23 @@ static void fill_ray_views(const ctgpu_scanner* s, int nViews, RayView* rv, floa
     }
 }
 
-// equiangular: the scanner's table of (cos, sin) of t * delta (built once)
+// equiangular: the scanner's tables of (cos, sin) of t * delta and of
+// t * delta / 2 (built once)
 static cudaError_t ensure_arc_table(ctgpu_scanner* s) {
   if (s->geometry != kEquiangular) return cudaSuccess;
   const int n = s->nDet * s->nSample;
   const double delta = s->angularDetInc / s->nSample;
   if (s->arcN == n && s->arcDelta == delta) return cudaSuccess;
   std::vector<double2> arc(n);
-  for (int t = 0; t < n; t++) arc[t] = make_double2(std::cos(t * delta), std::sin(t * delta));
+  std::vector<float2> half(n);
+  for (int t = 0; t < n; t++) {
+    arc[t] = make_double2(std::cos(t * delta), std::sin(t * delta));
+    half[t] = make_float2((float)std::cos(0.5 * t * delta), (float)std::sin(0.5 * t * delta));
+  }
   cudaError_t e = ensure_device(s->d_arc, s->d_arc_cap, (size_t)n);
   if (e == cudaSuccess) e = cudaMemcpy(s->d_arc, arc.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = ensure_device(s->d_half, s->d_half_cap, (size_t)n);
+  if (e == cudaSuccess) e = cudaMemcpy(s->d_half, half.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return e;
   s->arcN = n;
   s->arcDelta = delta;
@@ -758,6 +769,7 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
   L.views = reinterpret_cast<const RayView*>(s->d_stage);
   L.sdirs = par ? reinterpret_cast<const float2*>(s->d_stage + oD) : nullptr;
   L.arc = s->d_arc;
+  L.arcHalf = s->d_half;
   L.sino = d_sino;
   L.status = status_pointer();
   CUDA_TRY(ensure_device(s->d_records, s->d_records_cap, raysum_record_bytes(L, L.nElem)));
@@ -820,6 +832,7 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   L.views = reinterpret_cast<const RayView*>(s->d_stage);
   L.sdirs = par ? reinterpret_cast<const float2*>(s->d_stage + oD) : nullptr;
   L.arc = s->d_arc;
+  L.arcHalf = s->d_half;
   L.sino = d_sinos;
   L.status = status_pointer();
   L.nSlices = n;
@@ -883,6 +896,7 @@ int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ell, in
   L.views = s->d_views;
   L.sdirs = s->d_sdirs;
   L.arc = s->d_arc;
+  L.arcHalf = s->d_half;
   L.sino = d_sino;
   L.status = status_pointer();
   L.elemsPerView = 1;
@@ -923,6 +937,7 @@ int ctgpu_raysum_ellipse_gradient(ctgpu_scanner* s, const ctgpu_phantom* p,
   L.views = s->d_views;
   L.sdirs = s->d_sdirs;
   L.arc = s->d_arc;
+  L.arcHalf = s->d_half;
   std::vector<double> g(6 * (size_t)(n > 0 ? n : 1), 0.0);
   cudaError_t e = cudaMemsetAsync(d_grad, 0, sizeof(double) * g.size(), st);
   if (e == cudaSuccess) e = launch_raysum_ellipse_grad(L, d_gsino, d_grad, st);

@@ -73,6 +73,7 @@ struct RaysumLaunch {
   const RayView* views;   // nViews
   const float2* sdirs;    // parallel: [nViews][nSample] unit ray directions
   const double2* arc;     // equiangular: (cos, sin) of t * delta, t < nDet * nSample
+  const float2* arcHalf;  // equiangular: (cos, sin) of t * delta / 2 (FP32)
   void* records;          // scratch: raysum_record_bytes()
   float* sino;
   unsigned int* status;

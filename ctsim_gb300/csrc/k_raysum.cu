@@ -484,8 +484,10 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
         rx *= invr;
         ry *= invr;
       } else {
-        float half = ft * hdelta;    // phi_t / 2, phi_t = t * delta
-        sincosf(half, &sj, &cj);
+        // cos, sin of phi_t / 2 (phi_t = t * delta) from the scanner's table
+        const float2 cs = __ldg(&L.arcHalf[t]);
+        cj = cs.x;
+        sj = cs.y;
         float cphi = fmaf(-2.f * sj, sj, 1.f), sphi = 2.f * sj * cj;
         float dxv = CD * (fca0 * cphi - fsa0 * sphi), dyv = CD * (fsa0 * cphi + fca0 * sphi);
         rx = dxv - Sx;
