@@ -157,6 +157,38 @@ def test_filter_matches_oracle(gpu, oracle):
         assert e < TOL, (flt, meth, zp, gen, geo, e)
 
 
+@pytest.mark.parametrize("nd", [3, 64, 129, 367, 1500, 2049, 4500, 8192])
+def test_filter_sizes_against_oracle(gpu, oracle, nd):
+    """Every FFT filter kernel variant (transform lengths 8 to 16384: 128 to
+    1024 threads, radix-8 and radix-16 passes), with three views (the last
+    CTA's pair holds one), against the FP64 oracle; detectors past 8192 are
+    rejected."""
+    torch, cg, device = gpu
+    rng = np.random.default_rng(nd)
+    nv = 3
+    x = rng.random((nv, nd)).astype(np.float32)
+    xd = to_dev(torch, device, x)
+    g = cg.Geometry(1, nd, nv, 0, 0, 0.01, 0, 0.0021, 2.6, 2.6, 5.2, 1.0)
+    plan = device.ReconPlan(g, 16, 16, "abs_hamming", 0.54, "fft", 1, "direct", "linear", 1,
+                            "table")
+    out = device.alloc_sinogram(nv, nd)
+    plan.filter(xd, out)
+    cg.sync()
+    ref = oracle.ProcessSignal("abs_hamming", "fft", nd, 0.0021, param=0.54, generation="direct",
+                               zeropad=1, geometry="equiangular", focal_length=2.6,
+                               sdl=5.2).filter(x)
+    e = rel_l2(out[:, :nd].cpu().numpy(), ref)
+    assert e < TOL, (nd, e)
+    if nd == 8192:
+        big = 8193
+        gb = cg.Geometry(1, big, 1, 0, 0, 0.01, 0, 0.0021, 2.6, 2.6, 5.2, 1.0)
+        pb = device.ReconPlan(gb, 16, 16, "abs_hamming", 0.54, "fft", 1, "direct", "linear", 1,
+                              "table")
+        with pytest.raises(cg.CtgpuError) as ei:
+            pb.filter(device.alloc_sinogram(1, big), device.alloc_sinogram(1, big))
+        assert ei.value.code == 2
+
+
 def test_helical_bit_exact(gpu, golden):
     torch, cg, device = gpu
     d = golden("helical")
