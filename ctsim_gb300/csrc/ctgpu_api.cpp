@@ -1120,10 +1120,14 @@ int ctgpu_recon_image_axes(const ctgpu_recon* r, double extent[4], double increm
 void ctgpu_recon_destroy(ctgpu_recon* r) { delete r; }
 
 // Filtering of nBatch sinograms of nViews rows each, one launch.
+// narrowOk: a launch of few blocks may use the N / 8-thread transform (the
+// single-slice entry point; batched launches keep one arithmetic)
 static int recon_filter_batch(ctgpu_recon* r, const float* d_sino, int sinoPitch,
                               size_t sinoStride, int nViews, float* d_filtered, int filtPitch,
-                              size_t filtStride, int nBatch, cudaStream_t st) {
+                              size_t filtStride, int nBatch, cudaStream_t st,
+                              bool narrowOk = false) {
   FilterLaunch L{};
+  L.narrowOk = narrowOk ? 1 : 0;
   L.nDet = r->g.n_det;
   L.nViews = nViews;
   L.inPitch = sinoPitch;
@@ -1149,7 +1153,7 @@ int ctgpu_recon_filter(ctgpu_recon* r, const float* d_sino, int sinoPitch, int n
   if (!r || !d_sino || !d_filtered) return fail(CTGPU_ERR_INVALID, "null argument");
   if (sinoPitch < r->g.n_det || filtPitch < r->g.n_det) return fail(CTGPU_ERR_INVALID, "pitch < nDet");
   return recon_filter_batch(r, d_sino, sinoPitch, 0, nViews, d_filtered, filtPitch, 0, 1,
-                            (cudaStream_t)stream);
+                            (cudaStream_t)stream, true);
 }
 
 // The backprojection launch descriptor of a plan (Backproject::Backproject's

@@ -103,6 +103,9 @@ struct FilterLaunch {
   float* out;               // [nBatch][nViews][outPitch]
   int nBatch;
   size_t inSliceStride, outSliceStride;
+  // a launch of few blocks may give each transform N / 8 threads (the
+  // single-slice entry points; batched launches keep one arithmetic)
+  int narrowOk;
 };
 
 // Backprojection of one problem.

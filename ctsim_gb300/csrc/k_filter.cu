@@ -70,7 +70,20 @@ cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s) {
 #ifndef CTGPU_FILTER_WIDE
 #define CTGPU_FILTER_WIDE 16   // threads per block = N / CTGPU_FILTER_WIDE (two butterflies each)
 #endif
-  int T = N / CTGPU_FILTER_WIDE;
+  const int nBatch = L.nBatch > 0 ? L.nBatch : 1;
+  if (nBatch > 65535) return cudaErrorInvalidConfiguration;
+  const long long blocks = (long long)((L.nViews + 1) / 2) * nBatch;
+  // where allowed, a launch of fewer blocks than the SMs hold at four each
+  // (a single slice) gives each transform N / 8 threads: the blocks are then
+  // short, and the launch is as long as one block
+  static const int sms = [] {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      n = 1;
+    return n;
+  }();
+  int T = N / (L.narrowOk && blocks < 4LL * sms ? 8 : CTGPU_FILTER_WIDE);
   if (T < 32) T = 32;
   if (T > 1024) T = 1024;
   const bool one = T * 8 >= N;
@@ -85,8 +98,6 @@ cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s) {
                                          (int)smem);
     if (e != cudaSuccess) return e;
   }
-  const int nBatch = L.nBatch > 0 ? L.nBatch : 1;
-  if (nBatch > 65535) return cudaErrorInvalidConfiguration;
   dim3 grid((L.nViews + 1) / 2, nBatch);
   kern<<<grid, T, smem, s>>>(L);
   return cudaGetLastError();
