@@ -327,6 +327,9 @@ struct ctgpu_recon {
   unsigned char* d_scratch2 = nullptr;
   size_t d_scratch2_cap = 0;
   cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr, s_comp2 = nullptr;
+  // ctgpu_recon_run: the tile records' stream (beside the filter) and events
+  cudaStream_t s_side = nullptr;
+  cudaEvent_t sideEv[2] = {};
   cudaEvent_t ev[6] = {};   // in_done[2], comp_done[2], out_done[2]
   double* h_angles_pinned = nullptr;   // page-locked copy of the view angles
   size_t h_angles_cap = 0;
@@ -341,7 +344,9 @@ struct ctgpu_recon {
       if (p) cudaFree(p);
     for (cudaEvent_t e : ev)
       if (e) cudaEventDestroy(e);
-    for (cudaStream_t s : {s_in, s_comp, s_out, s_comp2})
+    for (cudaEvent_t e : sideEv)
+      if (e) cudaEventDestroy(e);
+    for (cudaStream_t s : {s_in, s_comp, s_out, s_comp2, s_side})
       if (s) cudaStreamDestroy(s);
   }
 };
@@ -1198,6 +1203,18 @@ static BackprojLaunch make_launch(const ctgpu_recon* r, int nViews, int pitch,
 }
 
 // Backprojection of nViews filtered rows; outScale multiplies this launch's sum.
+// a one-slice launch's view groups (table_view_groups on this device)
+static cudaError_t set_view_groups(ctgpu_recon* r, BackprojLaunch& L) {
+  if (!r->sms) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&r->sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+  }
+  L.viewGroups = table_view_groups(L, r->sms);
+  return cudaSuccess;
+}
+
 // reuseScratch: the scratch whose (tile, view) records an earlier launch on
 // stream st built for the same view angles (table family), or null;
 // anglesOnDevice: r->d_angles already holds h_angles, ordered before st's work;
@@ -1260,14 +1277,7 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
   }
   BackprojLaunch L = make_launch(r, nViews, pitch, r->d_angles, d_filtered, d_image, accumulate,
                                  outScale, nBatch, filtStride, imageStride);
-  if (splitViews && nBatch == 1) {
-    if (!r->sms) {
-      int dev = 0;
-      CUDA_TRY(cudaGetDevice(&dev));
-      CUDA_TRY(cudaDeviceGetAttribute(&r->sms, cudaDevAttrMultiProcessorCount, dev));
-    }
-    L.viewGroups = table_view_groups(L, r->sms);
-  }
+  if (splitViews && nBatch == 1) CUDA_TRY(set_view_groups(r, L));
   size_t sb = backproject_scratch_bytes(L);
   unsigned char* scratch = extScratch;
   bool stable = true;
@@ -1318,15 +1328,41 @@ int ctgpu_recon_run(ctgpu_recon* r, const float* d_sino, int sinoPitch, const do
   if (startView < 0 || startView + nViews > r->g.n_view) return fail(CTGPU_ERR_INVALID, "view range outside the projections");
   cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(ensure_device(r->d_filtered, r->d_filtered_cap, (size_t)nViews * r->pitch));
-  int rc = ctgpu_recon_filter(r, d_sino + (size_t)startView * sinoPitch, sinoPitch, nViews,
-                              r->d_filtered, r->pitch, stream);
-  if (rc) return rc;
   bool acc = (flags & CTGPU_RUN_ACCUMULATE) != 0;
   bool post = (flags & CTGPU_RUN_POSTPROCESS) != 0;
   float scale = raw_scale(r);
   if (post && !acc && r->bproj != kTrig) scale = (float)(scale * r->rotScale);   // fused PostProcessing
+  // table family: the (tile, view) records depend on the geometry and the
+  // angles only, so they are built on a side stream while the filter runs;
+  // the scratch is sized here as the backprojection below sizes it
+  const unsigned char* recs = nullptr;
+  if (nViews > 0 && r->bproj != kDiff && r->bproj != kIDiff) {
+    CUDA_TRY(ensure_device(r->d_angles, r->d_angles_cap, (size_t)nViews));
+    CUDA_TRY(cudaMemcpyAsync(r->d_angles, h_angles + startView, sizeof(double) * nViews,
+                             cudaMemcpyHostToDevice, st));
+    BackprojLaunch L = make_launch(r, nViews, r->pitch, r->d_angles, r->d_filtered, d_image,
+                                   acc ? 1 : 0, scale, 1, 0, 0);
+    CUDA_TRY(set_view_groups(r, L));
+    CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, backproject_scratch_bytes(L)));
+    if (!r->s_side) CUDA_TRY(cudaStreamCreateWithFlags(&r->s_side, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : r->sideEv)
+      if (!e) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventRecord(r->sideEv[0], st));   // angles up; the last call's work queued
+    CUDA_TRY(cudaStreamWaitEvent(r->s_side, r->sideEv[0], 0));
+    cudaError_t e = launch_tile_setup(L, r->d_scratch, r->s_side);
+    if (e == cudaErrorInvalidValue)
+      return fail(CTGPU_ERR_UNSUPPORTED, "image pixels behind the fan-beam source");
+    CUDA_TRY(e);
+    CUDA_TRY(cudaEventRecord(r->sideEv[1], r->s_side));
+    recs = r->d_scratch;
+  }
+  int rc = ctgpu_recon_filter(r, d_sino + (size_t)startView * sinoPitch, sinoPitch, nViews,
+                              r->d_filtered, r->pitch, stream);
+  if (rc) return rc;
+  if (recs) CUDA_TRY(cudaStreamWaitEvent(st, r->sideEv[1], 0));
   rc = recon_backproject_scaled(r, r->d_filtered, r->pitch, h_angles + startView, nViews, d_image,
-                                acc ? 1 : 0, scale, st, 1, 0, 0, nullptr, false, nullptr, true);
+                                acc ? 1 : 0, scale, st, 1, 0, 0, recs, recs != nullptr, nullptr,
+                                true);
   if (rc) return rc;
   if (post && acc) return ctgpu_recon_postprocess(r, d_image, stream);
   return ok();

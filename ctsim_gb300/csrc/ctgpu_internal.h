@@ -254,6 +254,8 @@ bool table_prep_info(const BackprojLaunch& L, TablePrep* out);
 // interval rows and (tile, view) records of one problem into scratch
 cudaError_t launch_table_prep(const BackprojLaunch& L, const TablePrep& P, void* scratch,
                               cudaStream_t s);
+// the (tile, view) records alone (geometry and view angles only)
+cudaError_t launch_tile_setup(const BackprojLaunch& L, void* scratch, cudaStream_t s);
 
 struct BatchProblem {
   BackprojLaunch L;   // one slice: nBatch 1
