@@ -373,9 +373,14 @@ def test_batch_host_chunks_share_records(gpu, geo, interp, backproj):
     assert plan.host_chunks(B) == planned
 
 
-@pytest.mark.parametrize("geo,n,interp", [("equiangular", 512, "cubic"), ("parallel", 256, "linear"),
-                                          ("equilinear", 128, "nearest"), ("parallel", 96, "cubic")])
-def test_single_slice_view_groups(gpu, geo, n, interp):
+@pytest.mark.parametrize("geo,n,interp,bp", [("equiangular", 512, "cubic", "table"),
+                                             ("parallel", 256, "linear", "table"),
+                                             ("equilinear", 128, "nearest", "table"),
+                                             ("parallel", 96, "cubic", "table"),
+                                             ("parallel", 512, "linear", "idiff"),
+                                             ("parallel", 256, "nearest", "idiff"),
+                                             ("parallel", 128, "cubic", "idiff")])
+def test_single_slice_view_groups(gpu, geo, n, interp, bp):
     """A single slice of few tiles splits its views into groups whose partial
     images are summed in order: the same image as the batched (unsplit)
     launch to FP32 rounding, also when the views come in two accumulated
@@ -388,7 +393,7 @@ def test_single_slice_view_groups(gpu, geo, n, interp):
     sino = device.alloc_sinogram(nv, nd)
     ang = device.raysums(sc, ph, sino)
     plan = device.ReconPlan(sc.geometry(), n, n, "abs_hamming", 0.54, "fft", 2, "direct", interp,
-                            1, "table")
+                            1, bp)
     one = torch.zeros((n, n), device="cuda")
     plan.run(sino, ang, one)
     batch = torch.zeros((2, n, n), device="cuda")
