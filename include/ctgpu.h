@@ -193,7 +193,11 @@ int ctgpu_recon_backproject(ctgpu_recon* r, const float* d_filtered, int filtere
 int ctgpu_recon_postprocess(ctgpu_recon* r, float* d_image, void* stream);
 /* Reconstructor::reconstructView(start, count) (+ postProcessing when
  * CTGPU_RUN_POSTPROCESS is set, i.e. reconstructAllViews). d_sino holds all
- * n_view rows; h_view_angles all n_view angles. */
+ * n_view rows; h_view_angles all n_view angles.  One slice fills few blocks,
+ * so this call (and ctgpu_recon_run_host, ctgpu_recon_backproject) may split
+ * the views into groups whose partial images are summed in a fixed order, and
+ * filter with another transform split: its image equals the batched entry
+ * points' to FP32 rounding (deterministic from call to call). */
 #define CTGPU_RUN_POSTPROCESS 1
 #define CTGPU_RUN_ACCUMULATE 2
 int ctgpu_recon_run(ctgpu_recon* r, const float* d_sino, int sino_pitch,
