@@ -167,6 +167,30 @@ def cpu_fbp_rate(seed, seconds=10.0, nthreads=None, views=None):
         done, nv, nthreads, el), nthreads
 
 
+def oracle_parity(elems0, elems, g, sino, image, angles):
+    """One slice of the timed batch against the FP64 oracle: its ray-sums
+    (scanner geometry from the batch's first phantom, as on the device) and
+    the oracle's FBP of the same FP32 sinogram the device read.  The oracle
+    is the checker here; nothing timed runs through it."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "oracle"], check=True)
+    import pyoracle as po
+    osc = po.Scanner(po.Phantom(elements=elems0), "equiangular", N_DET, N_VIEW, nsample=1)
+    osc.phantom = po.Phantom(elements=elems)
+    s_ref, a_ref = osc.collect()
+    s_gpu = sino[:, :N_DET].cpu().numpy().astype(np.float64)
+    ref = po.reconstruct(osc.geom(), s_gpu.astype(np.float32), angles, NX, NX,
+                         filter_name="abs_hamming", param=0.54, method="fft", zeropad=2,
+                         backproj="table", interp="cubic")
+    img = image.cpu().numpy().astype(np.float64)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    return {"sinogram_rel_l2": rel(s_gpu, s_ref), "image_rel_l2": rel(img, ref),
+            "angles_equal": bool(np.array_equal(np.asarray(angles), a_ref)),
+            "tolerance": 1e-5}
+
+
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -561,8 +585,8 @@ def run_gpu(args):
     B = args.batch
     stream = torch.cuda.current_stream()
     # --- inputs: B seeded phantoms, simulated on the device --------------------
-    phs = [phantoms.make_phantom(phantoms.random_ellipses(seed=rank * 100000 + b, n=12))
-           for b in range(B)]
+    elems = [phantoms.random_ellipses(seed=rank * 100000 + b, n=12) for b in range(B)]
+    phs = [phantoms.make_phantom(e) for e in elems]
     # one scanner (its geometry from the first phantom) scans every phantom
     sc = cg.Scanner(phs[0], "equiangular", N_DET, N_VIEW, nSample=1)
     g = sc.geometry()
@@ -678,6 +702,8 @@ def run_gpu(args):
     traffic = traffic_per_launch(B)
     cpu_v, cpu_sample, cpu_threads = cpu_fbp_rate(seed=7, seconds=args.cpu_seconds,
                                                   views=args.ref_views)
+    parity = oracle_parity(elems[0], elems[B - 1], g, sinos[B - 1], images[B - 1], angles[0])
+    parity["slice"] = B - 1
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": fbp_ms / steps, "higher_is_better": True,
@@ -727,6 +753,7 @@ def run_gpu(args):
                                         (sms * 128 * sm_mhz * 1e6 / 1e9)}},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                          "sample": cpu_sample},
+        "parity_vs_fp64_oracle": parity,
         "e2e": {"value": PV_PER_SLICE * B * e2e_steps * world / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": B * N_VIEW * N_DET * 4 + len(e2e_chunks) * N_VIEW * 8,
                 "d2h_bytes_per_step": B * NX * NX * 4,

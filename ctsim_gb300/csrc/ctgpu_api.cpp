@@ -476,8 +476,7 @@ int ctgpu_scanner_create(const ctgpu_phantom* p, const char* geometry_name, int 
   s->geometry = geom; s->nDet = nDet; s->nView = nView; s->offsetView = offsetView;
   s->nSample = nSample;
   // Scanner::Scanner (scanner.cpp:110-222)
-  double maxAxis = std::fmax(p->xmax - p->xmin, p->ymax - p->ymin);
-  maxAxis = (p->xmax - p->xmin) > (p->ymax - p->ymin) ? (p->xmax - p->xmin) : (p->ymax - p->ymin);
+  double maxAxis = (p->xmax - p->xmin) > (p->ymax - p->ymin) ? (p->xmax - p->xmin) : (p->ymax - p->ymin);
   s->viewDiameter = kSqrt2 * maxAxis * viewRatio;
   s->focalLength = (s->viewDiameter / 2) * flRatio;
   s->centerDetectorLength = (s->viewDiameter / 2) * cdRatio;
@@ -1062,6 +1061,11 @@ int ctgpu_recon_create(const ctgpu_geometry* g, int nx, int ny, const char* filt
   if (bp < 0) return fail(CTGPU_ERR_INVALID, std::string("Error creating backprojector: Invalid backprojection name ") + backprojName);
   if (ip < 0) return fail(CTGPU_ERR_INVALID, std::string("Error creating backprojector: Invalid interpolation name ") + interpName);
   if (interpFactor < 1) return fail(CTGPU_ERR_INVALID, "interpolation factor must be >= 1");
+  // The reference's preinterpolation factor has defined semantics only inside
+  // its FFTW filter (procsignal.cpp:600-626, unavailable to pin) and scales
+  // idiff's nearest index (backprojectors.cpp:627); no other path reads it.
+  if (interpFactor != 1)
+    return fail(CTGPU_ERR_UNSUPPORTED, "preinterpolation factor other than 1 is not supported");
   FilterSpec sp{};
   sp.filterId = fid; sp.method = mid; sp.generation = gid; sp.zeropad = zeropad;
   sp.interpFactor = interpFactor; sp.geometry = g->geometry; sp.nDet = g->n_det;

@@ -1,8 +1,7 @@
 // k_noalloc.cu -- the "diff" backprojection with its scratch in a fixed,
 // file-scope device array, for callers that cannot allocate device memory.
 //
-// Some callers of this library cannot call cudaMalloc: code running inside a
-// CUDA-graph capture that must not grow the memory pool, plug-ins hosted by an
+// Some callers of this library cannot call cudaMalloc: plug-ins hosted by an
 // application that owns every device allocation (its own allocator or a fixed
 // memory budget), and real-time loops that must not block on the allocator.
 // ctgpu_backproject_diff_noalloc() serves them: the caller passes the filtered
@@ -14,9 +13,10 @@
 // address is looked up once per device, on that device's first call (see the
 // entry point's comment in include/ctgpu.h).  All calls share the array and it
 // keeps the last call's contents; each call writes every element it later
-// reads (the view records from the host, the row ranges by the set-up kernel),
-// so nothing needs clearing.  Calls that overlap on the GPU (different streams
-// or threads) race on the array.
+// reads (the view records by a small kernel whose parameters carry them, the
+// row ranges by the set-up kernel), so nothing needs clearing.  Calls that
+// overlap on the GPU (different streams or threads) race on the array.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -28,6 +28,17 @@
 namespace ctgpu {
 struct DiffViewRecord { double dx, dy, colStart; };   // layout of k_backproject.cu's DiffView
 struct DiffColRecord { double c0; int a, b; };        // layout of k_backproject.cu's DiffCol
+
+// Up to kViewsPerParamBlock view records travel by value as one kernel's
+// parameters (3 KB of the 4 KB parameter space), so no host buffer is read
+// after the launch call returns and no host-to-device copy is queued.
+constexpr int kViewsPerParamBlock = 128;
+struct DiffViewParams { DiffViewRecord r[kViewsPerParamBlock]; };
+
+__global__ void noalloc_store_views_kernel(DiffViewParams p, int n, DiffViewRecord* dst) {
+  int i = threadIdx.x;
+  if (i < n) dst[i] = p.r[i];
+}
 }  // namespace ctgpu
 
 using namespace ctgpu;
@@ -45,19 +56,21 @@ int fail(int code, const std::string& msg) {
 // Device address of g_noalloc_scratch on the current device, looked up once per
 // device with that device current.  Host code must not use the symbol itself:
 // on the host it is only a stand-in, not a device address.
+// Concurrent first calls from several host threads may both look the address
+// up; they store the same value, and the atomics make that well defined.
 cudaError_t scratch_address(unsigned char** out) {
-  static unsigned char* ptrs[64] = {nullptr};
+  static std::atomic<unsigned char*> ptrs[64];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (!ptrs[dev]) {
-    unsigned char* ptr = nullptr;
+  unsigned char* ptr = ptrs[dev].load(std::memory_order_acquire);
+  if (!ptr) {
     e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    ptrs[dev] = ptr;
+    ptrs[dev].store(ptr, std::memory_order_release);
   }
-  *out = ptrs[dev];
+  *out = ptr;
   return cudaSuccess;
 }
 
@@ -109,19 +122,21 @@ extern "C" int ctgpu_backproject_diff_noalloc(const ctgpu_geometry* g, int nx, i
   const double startR = std::sqrt(x0 * x0 + y0 * y0), startPhi = std::atan2(y0, x0);
 
   // per-view steps (BackprojectDiff::BackprojectView, backprojectors.cpp:522-527),
-  // staged through a stack buffer into the scratch array
-  DiffViewRecord chunk[256];
-  for (int v0 = 0; v0 < n_views; v0 += 256) {
-    int nv = n_views - v0 < 256 ? n_views - v0 : 256;
+  // computed on the host in FP64 like the allocating path's, and stored into
+  // the scratch array by kernels that receive them as parameters
+  DiffViewParams blk;
+  for (int v0 = 0; v0 < n_views; v0 += kViewsPerParamBlock) {
+    int nv = n_views - v0 < kViewsPerParamBlock ? n_views - v0 : kViewsPerParamBlock;
     for (int i = 0; i < nv; i++) {
       double th = h_view_angles[v0 + i];
-      chunk[i].dx = xInc * std::cos(th) / g->det_inc;
-      chunk[i].dy = yInc * std::sin(th) / g->det_inc;
-      chunk[i].colStart = iDetCenter + startR * std::cos(th - startPhi) / g->det_inc;
+      blk.r[i].dx = xInc * std::cos(th) / g->det_inc;
+      blk.r[i].dy = yInc * std::sin(th) / g->det_inc;
+      blk.r[i].colStart = iDetCenter + startR * std::cos(th - startPhi) / g->det_inc;
     }
-    e = cudaMemcpyAsync(scratch + sizeof(DiffViewRecord) * v0, chunk, sizeof(DiffViewRecord) * nv,
-                        cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return fail(CTGPU_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+    noalloc_store_views_kernel<<<1, kViewsPerParamBlock, 0, st>>>(
+        blk, nv, (DiffViewRecord*)scratch + v0);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(CTGPU_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
   }
   BackprojLaunch L{};
   L.geometry = kParallel;

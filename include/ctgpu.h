@@ -494,9 +494,9 @@ int ctgpu_image_arith(const char* op, const float* d_a, const float* d_b, float*
 /* ------------------------------------------------------------------------ */
 /* No counterpart in the reference.  The "diff" backprojection of
  * ctgpu_recon_backproject for callers that cannot allocate device memory --
- * code inside a CUDA-graph capture that must not grow the memory pool,
- * plug-ins whose host application owns every device allocation, real-time
- * loops that must not block on the allocator.  It calls no cudaMalloc,
+ * plug-ins whose host application owns every device allocation (its own
+ * allocator or a fixed memory budget), real-time loops that must not block on
+ * the allocator.  It calls no cudaMalloc,
  * cudaFree or other allocating routine: the per-view steps and per-(view,
  * column) row ranges the diff backprojector needs live in a fixed 16 MiB
  * device array inside the library, which every GPU that loads the library
@@ -511,7 +511,9 @@ int ctgpu_image_arith(const char* op, const float* d_a, const float* d_b, float*
  * device current; make that first call before any stream capture.  All calls
  * share the array and it keeps the last call's contents (each call rewrites
  * everything it reads); calls that overlap on the GPU, on different streams
- * or threads, race on it. */
+ * or threads, race on it.  The view angles are read on the host during the
+ * call; the per-view steps reach the array as kernel parameters, so no host
+ * buffer is read after the call returns. */
 int ctgpu_backproject_diff_noalloc(const ctgpu_geometry* g, int nx, int ny,
                                    const char* interp_name, const ctgpu_roi* roi,
                                    const float* d_filtered, int filtered_pitch,

@@ -49,3 +49,19 @@ def test_errors_without_gpu_work():
         cg.Scanner(p, "equiangular", 11, 10, focalLengthRatio=0.5)
     with pytest.raises(cg.CtgpuError, match="Unknown PhantomElement type"):
         p.add_element("hexagon", 0, 0, 1, 1, 0, 1)
+
+
+def test_preinterpolation_factor_rejected_without_gpu_work():
+    """A preinterpolation factor other than 1 is refused on the host (the
+    reference gives it meaning only in its FFTW filter, which cannot be
+    pinned, and in idiff's nearest index)."""
+    import ctsim_gb300 as cg
+    from ctsim_gb300 import _lib, device
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("libctgpu.so not built")
+    g = cg.Geometry(0, 65, 48, 0, 0.0, 0.06544984694978735, -0.5, 0.0176, 1.1, 0.0, 0.0, 0.0)
+    for method in ("convolution", "fft", "fourier"):
+        with pytest.raises(cg.CtgpuError, match="preinterpolation factor") as ei:
+            device.ReconPlan(g, 32, 32, "abs_bandlimit", -1.0, method, 1, "direct", "linear", 2,
+                             "idiff")
+        assert ei.value.code == 2

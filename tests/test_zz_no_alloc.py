@@ -1,9 +1,11 @@
 """The allocation-free diff backprojection, for callers that cannot allocate
-device memory (graph capture that must not grow the pool, host applications
-that own every device allocation, real-time loops), against the library's
+device memory (host applications that own every device allocation, real-time
+loops that must not block on the allocator), against the library's
 allocating entry point: ctgpu_backproject_diff_noalloc vs
 ctgpu_recon_backproject with a "diff" plan, through the C ABI, two different
-calls in a row (the fixed scratch keeps the first call's contents)."""
+calls in a row (the fixed scratch keeps the first call's contents); then 720
+views (several blocks of view records), a region of interest, nearest
+interpolation and a view range accumulated onto an earlier one."""
 import ctypes as C
 
 import numpy as np
@@ -51,6 +53,51 @@ def test_noalloc_diff_matches_allocating_path(golden):
             C.c_void_p(out.data_ptr()), RUN_POSTPROCESS, device.stream_handle()))
         cg.sync()
         assert rel_l2(out.cpu().numpy(), ref.cpu().numpy()) < 1e-6, name
+
+
+def _noalloc(lib, g, nx, ny, interp, roi, filtered, ang, out, flags, stream):
+    from ctsim_gb300._lib import Roi, check
+    r = None if roi is None else C.byref(Roi(*roi))
+    check(lib().ctgpu_backproject_diff_noalloc(
+        C.byref(g), nx, ny, interp.encode(), r, C.c_void_p(filtered.data_ptr()),
+        filtered.shape[1], ang.ctypes.data_as(C.c_void_p), len(ang),
+        C.c_void_p(out.data_ptr()), flags, stream))
+
+
+def test_noalloc_many_views_roi_nearest_and_accumulate():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import ctsim_gb300 as cg
+    from ctsim_gb300 import device
+    from ctsim_gb300._lib import RUN_ACCUMULATE, RUN_POSTPROCESS, lib
+    ph = cg.Phantom("shepp-logan")
+    sc = cg.Scanner(ph, "parallel", 129, 720, nSample=1)
+    g = sc.geometry()
+    sino = device.alloc_sinogram(720, 129)
+    ang = np.ascontiguousarray(device.raysums(sc, ph, sino), np.float64)
+    nx, ny = 64, 48
+    roi = (-0.45, -0.3, 0.55, 0.62)
+    sh = device.stream_handle()
+    for interp, r in (("nearest", roi), ("cubic", roi), ("linear", None)):
+        plan = device.ReconPlan(g, nx, ny, "abs_bandlimit", -1.0, "convolution", 1, "direct",
+                                interp, 1, "diff", roi=r)
+        filtered = device.alloc_sinogram(720, 129)
+        plan.filter(sino, filtered)
+        ref = torch.zeros((nx, ny), device="cuda")
+        plan.backproject(filtered, ang, ref)
+        raw = ref.clone()
+        plan.postprocess(ref)
+        out = torch.full((nx, ny), 7.0, device="cuda")
+        _noalloc(lib, g, nx, ny, interp, r, filtered, ang, out, RUN_POSTPROCESS, sh)
+        cg.sync()
+        assert rel_l2(out.cpu().numpy(), ref.cpu().numpy()) < 1e-6, (interp, r)
+        # views [0, 300) and then [300, 720) added onto them, without PostProcessing
+        acc = torch.full((nx, ny), 7.0, device="cuda")
+        _noalloc(lib, g, nx, ny, interp, r, filtered[:300], ang[:300], acc, 0, sh)
+        _noalloc(lib, g, nx, ny, interp, r, filtered[300:], ang[300:], acc, RUN_ACCUMULATE, sh)
+        cg.sync()
+        assert rel_l2(acc.cpu().numpy(), raw.cpu().numpy()) < 1e-6, (interp, r)
 
 
 def test_noalloc_rejects_oversized_requests():
