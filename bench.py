@@ -152,10 +152,12 @@ def cpu_fbp_rate(seed, seconds=10.0, nthreads=None, views=None):
     t0 = time.perf_counter()
     sino, ang = sc.collect(nthreads=nthreads)
     cpu_raysum_rate[0] = RAYS_PER_SLICE / (time.perf_counter() - t0)
-    nv = N_VIEW if views is None else views
+    nv = N_VIEW if views is None else min(views, N_VIEW)
+    geom = sc.geom()
+    geom.nView = nv   # the oracle reads geom.nView rows
     done, t0 = 0, time.perf_counter()
     while True:
-        po.reconstruct(sc.geom(), sino[:nv].astype(np.float32), ang[:nv], NX, NX,
+        po.reconstruct(geom, np.ascontiguousarray(sino[:nv], np.float32), ang[:nv], NX, NX,
                        filter_name="abs_hamming", param=0.54, method="fft", zeropad=2,
                        backproj="table", interp="cubic", nthreads=nthreads)
         done += 1

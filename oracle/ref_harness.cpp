@@ -9,7 +9,7 @@
 //   ref_harness bp      PJFILE filtered.f64 NX NY BACKPROJ INTERP out.f64
 //       Backprojector::BackprojectView per view + PostProcessing
 //       (libctsim/backprojectors.cpp:109-121)
-//   ref_harness timerec PJFILE NX NY FILTER METHOD BACKPROJ INTERP NTHREADS [NVIEWS]
+//   ref_harness timerec PJFILE NX NY FILTER METHOD BACKPROJ INTERP NTHREADS [NVIEWS [PARAM [ZEROPAD]]]
 //       times Reconstructor over the first NVIEWS views, split across NTHREADS
 //       threads the way the GUI's worker threads do (one Reconstructor and one
 //       private image per thread, images summed: src/threadrecon.cpp:176-255)
@@ -97,6 +97,8 @@ static int cmdTimeRec(int argc, char** argv) {
   int nThreads = atoi(argv[9]);
   int nViews = argc > 10 ? atoi(argv[10]) : pj.nView();
   if (nViews > pj.nView()) nViews = pj.nView();
+  double param = argc > 11 ? atof(argv[11]) : -1;
+  int zeropad = argc > 12 ? atoi(argv[12]) : 1;
   std::vector<ImageFile*> ims(nThreads);
   auto t0 = std::chrono::steady_clock::now();
 #pragma omp parallel num_threads(nThreads)
@@ -106,7 +108,7 @@ static int cmdTimeRec(int argc, char** argv) {
     int start = t * per + (t < extra ? t : extra);
     int count = per + (t < extra ? 1 : 0);
     ims[t] = new ImageFile(nx, ny);
-    Reconstructor rec(pj, *ims[t], filt, -1, method, 1, "direct", interp, 1, bproj, 0);
+    Reconstructor rec(pj, *ims[t], filt, param, method, zeropad, "direct", interp, 1, bproj, 0);
     if (count > 0) rec.reconstructView(start, count);
     rec.postProcessing();
   }

@@ -252,6 +252,38 @@ def make_polar(tmp):
     np.savez_compressed(os.path.join(HERE, "polar.npz"), **out)
 
 
+# Phantom files read by the reference (Phantom::createFromFile): every element
+# type with non-zero attenuation (elements.phm, committed beside this script),
+# and one seeded random-ellipse phantom as the benchmarks draw them
+PHM_SCANS = [  # (name, phm file, geometry, ndet, nview, nray)
+    ("el_par", "elements", "parallel", 121, 90, 2),
+    ("el_eqa", "elements", "equiangular", 120, 96, 2),
+    ("el_eql", "elements", "equilinear", 131, 100, 2),
+    ("rnd_eqa", "random12", "equiangular", 129, 120, 1),
+]
+
+
+def make_phmfile(tmp):
+    from ctsim_gb300.phantoms import random_ellipses, write_phm
+    files = {"elements": os.path.join(HERE, "elements.phm"),
+             "random12": os.path.join(tmp, "random12.phm")}
+    write_phm(files["random12"], random_ellipses(seed=2, n=12))
+    out = {"random12/text": np.array(open(files["random12"]).read())}
+    for name, phm, geo, nd, nv, nr in PHM_SCANS:
+        f = os.path.join(tmp, name + ".pj")
+        run(REF, "phm2pj", f, nd, nv, "--phmfile", files[phm], "--geometry", geo, "--nray", nr)
+        out.update(pj_arrays(name + "/", read_pj(f)))
+        out[name + "/cfg"] = np.array([phm, geo, nd, nv, nr], dtype=object)
+    for k, (n, ns) in enumerate([(48, 2), (37, 3)]):
+        f = os.path.join(tmp, "p.if")
+        run(REF64, "phm2if", f, n, n, "--phmfile", files["elements"], "--nsample", ns)
+        out["raster%d/image" % k] = read_if(f).data
+        run(REF, "phm2if", f, n, n, "--phmfile", files["elements"], "--nsample", ns)
+        out["raster%d/image32" % k] = read_if(f).data
+        out["raster%d/cfg" % k] = np.array([n, ns])
+    np.savez_compressed(os.path.join(HERE, "phmfile.npz"), **out)
+
+
 def main():
     for b in (REF, REF64, HARN):
         if not os.path.exists(b):
@@ -272,6 +304,8 @@ def main():
             make_io(tmp)
         if not only or "polar" in only:
             make_polar(tmp)
+        if not only or "phmfile" in only:
+            make_phmfile(tmp)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print("%-14s %8d bytes" % (f, os.path.getsize(os.path.join(HERE, f))))

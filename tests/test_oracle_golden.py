@@ -167,3 +167,47 @@ def test_oracle_convert_polar_matches_reference(oracle, golden, k):
                                d["%d/angles" % k], int(nx), int(ny), interp)
     c = min(int(nx), int(ny))
     np.testing.assert_array_equal(out[:c], d["%d/image" % k][:c])
+
+
+PHM_FILES = {"elements": ("tests", "golden", "elements.phm")}
+
+
+def test_oracle_phantom_file_raysums_match_reference(oracle, golden, tmp_path):
+    """Phantom files (Phantom::createFromFile) with every element type at
+    non-zero attenuation -- rectangles, sectors, a segment, a triangle, an
+    ellipse -- and a seeded random-ellipse phantom written by
+    phantoms.write_phm, scanned by the reference's phm2pj --phmfile."""
+    import os
+    from conftest import ROOT
+    from ctsim_gb300.phantoms import random_ellipses, write_phm
+    d = golden("phmfile")
+    rnd = tmp_path / "random12.phm"
+    write_phm(str(rnd), random_ellipses(seed=2, n=12))
+    assert rnd.read_text() == str(d["random12/text"])   # the seeded draw is reproducible
+    files = {"elements": os.path.join(ROOT, *PHM_FILES["elements"]), "random12": str(rnd)}
+    types = {e[0] for e in oracle.read_phm(files["elements"])}
+    assert types == {"rectangle", "sector", "segment", "triangle", "ellipse"}
+    for name in ("el_par", "el_eqa", "el_eql", "rnd_eqa"):
+        phm, geo, nd, nv, nr = d[name + "/cfg"]
+        sc = oracle.Scanner(oracle.Phantom(filename=files[phm]), geo, int(nd), int(nv),
+                            nsample=int(nr))
+        hdr = d[name + "/hdr"]
+        assert sc.detInc == hdr[6] and sc.viewDiameter == hdr[7] and sc.fanBeamAngle == hdr[10]
+        sino, ang = sc.collect()
+        np.testing.assert_array_equal(ang, d[name + "/angles"])
+        ref = d[name + "/data"]
+        assert np.abs(ref).max() > 0.1
+        mism = np.count_nonzero(sino.astype(np.float32) != ref)
+        assert mism <= max(1, ref.size // 100000), (name, mism)
+        assert rel_l2(sino, ref) < 1e-7, name
+
+
+def test_oracle_phantom_file_raster_matches_reference(oracle, golden):
+    import os
+    from conftest import ROOT
+    d = golden("phmfile")
+    ph = oracle.Phantom(filename=os.path.join(ROOT, *PHM_FILES["elements"]))
+    for k in range(2):
+        n, ns = d["raster%d/cfg" % k]
+        img, _ = oracle.phantom_to_image(ph, int(n), int(n), 1.0, int(ns))
+        np.testing.assert_allclose(img, d["raster%d/image" % k], rtol=0, atol=1e-12)
