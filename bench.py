@@ -55,6 +55,25 @@ def peaks():
     return 6800.0, "fallback", 2070.0
 
 
+def measured_device_peaks(stream_handle):
+    """FP32 FMA and gather-bandwidth peaks measured on this GPU by the
+    microkernels of libctpeaks.so (ctsim_gb300/csrc/peaks/k_peaks.cu), CUDA
+    events, best of 5 launches each."""
+    import ctypes as C
+    path = os.path.join(ROOT, "ctsim_gb300", "libctpeaks.so")
+    lib = C.CDLL(path)
+    lib.ctpeaks_measure.argtypes = [C.c_void_p, C.c_void_p]
+    out = (C.c_double * 8)()
+    if lib.ctpeaks_measure(out, stream_handle) != 0:
+        raise RuntimeError("ctpeaks_measure failed")
+    return {"ffma_tflops": out[0], "ffma2_tflops": out[1], "lds128_gbs": out[2],
+            "l2_gather16_gbs": out[3], "l2_read_gbs": out[4], "sms": int(out[5]),
+            "how": "CUDA events, best of 5: scalar FFMA and packed FFMA2 (8 chains/thread, "
+                   "4 x 256 threads/SM); LDS.128 of consecutive 16-B words; 16-B "
+                   "pseudo-random gathers and coalesced 16-B reads from a 16 MiB "
+                   "L2-resident buffer (ld.global.cg)"}
+
+
 def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
         int(os.environ.get("LOCAL_RANK", 0))
@@ -225,16 +244,19 @@ def traffic_per_launch(batch):
     batch size; the traffic grows in proportion to the slices)."""
     p = os.path.join(ROOT, "profiles", "backproject_equiangular_cubic_512_ncu.md")
     if not os.path.exists(p):
-        return None
+        return None, None
     vals = {}
     with open(p) as f:
         for line in f:
-            for key in ("traffic_bytes_per_launch:", "traffic_batch_slices:"):
+            for key in ("traffic_bytes_per_launch:", "traffic_batch_slices:", "captured_at_commit:"):
                 if line.startswith(key):
-                    vals[key] = float(line.split(":")[1])
+                    vals[key] = line.split(":", 1)[1].strip()
     if "traffic_bytes_per_launch:" not in vals or "traffic_batch_slices:" not in vals:
-        return None
-    return vals["traffic_bytes_per_launch:"] * batch / vals["traffic_batch_slices:"]
+        return None, None
+    src = "profiles/backproject_equiangular_cubic_512_ncu.md, captured at commit %s" % \
+        vals.get("captured_at_commit:", "unknown")
+    return (float(vals["traffic_bytes_per_launch:"]) * batch /
+            float(vals["traffic_batch_slices:"]), src)
 
 
 def batched_uneven(args, torch, cg, device, phantoms, rank):
@@ -586,8 +608,15 @@ def run_gpu(args):
         torch.cuda.set_device(0)
     B = args.batch
     stream = torch.cuda.current_stream()
+    from ctsim_gb300 import sharding
+    # views: every rank holds its view block of the same B slices and the
+    # partial images are summed (NCCL) inside the step; problems: each rank
+    # reconstructs its own B slices of a global batch of B x world
+    shard_views = world > 1 and args.shard == "views"
+    v0, vc = sharding.view_block(N_VIEW, rank, world) if shard_views else (0, N_VIEW)
     # --- inputs: B seeded phantoms, simulated on the device --------------------
-    elems = [phantoms.random_ellipses(seed=rank * 100000 + b, n=12) for b in range(B)]
+    first = 0 if shard_views else sharding.problem_block(B * world, rank, world)[0]
+    elems = [phantoms.random_ellipses(seed=first + b, n=12) for b in range(B)]
     phs = [phantoms.make_phantom(e) for e in elems]
     # one scanner (its geometry from the first phantom) scans every phantom
     sc = cg.Scanner(phs[0], "equiangular", N_DET, N_VIEW, nSample=1)
@@ -599,11 +628,28 @@ def run_gpu(args):
     plan = device.ReconPlan(g, NX, NX, "abs_hamming", 0.54, "fft", 2, "direct", "cubic", 1, "table")
     angles = [None]
 
+    block = torch.zeros((B, vc, pitch), device="cuda") if shard_views else None
+    fblock = torch.zeros_like(block) if shard_views else None
+
     def raysum_step():
         # every phantom's ray-sums in one launch
         angles[0] = device.raysums_batch(sc, phs, sinos)
 
     def fbp_step(bp_events=None):
+        if shard_views:
+            # this rank's view block of every slice: one filter launch, one
+            # batched backprojection without PostProcessing, the image sum
+            # over the ranks, PostProcessing
+            plan.filter(block.view(B * vc, pitch), fblock.view(B * vc, pitch))
+            if bp_events is not None:
+                bp_events[0].record(stream)
+            plan.backproject_batch(fblock, angles[0][v0:v0 + vc], images, postprocess=False)
+            if bp_events is not None:
+                bp_events[1].record(stream)
+            sharding.reduce_partial_images(images)
+            for b in range(B):
+                plan.postprocess(images[b])
+            return
         # one filter launch for the batch's B x n_view rows, then the batch's
         # backprojection (interval rows, tile records, backprojection)
         plan.filter(sinos.view(B * N_VIEW, pitch), filtered.view(B * N_VIEW, pitch))
@@ -615,8 +661,12 @@ def run_gpu(args):
 
     for _ in range(max(args.warmup, 1)):
         raysum_step()
+        if shard_views:
+            block.copy_(sinos[:, v0:v0 + vc])
         fbp_step()
     cg.sync()
+    dev_peaks = measured_device_peaks(device.stream_handle())
+    torch.cuda.synchronize()
 
     # --- timed: FBP --------------------------------------------------------------
     bp_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -654,21 +704,41 @@ def run_gpu(args):
     # ctgpu_recon_run_batch_host overlaps the copies of one chunk with the
     # reconstruction of the previous one and returns when the images are in
     # host memory
-    host_sinos = sinos[:, :, :N_DET].contiguous().cpu().pin_memory()
     host_images = torch.zeros((B, NX, NX), dtype=torch.float32).pin_memory()
-    e2e_chunks = plan.host_chunks(B)
-    plan.run_batch_host(host_sinos, angles[0], host_images)
+    if shard_views:
+        # this rank's view block from page-locked host memory, the sharded
+        # step (image sum inside), the images back to the host
+        host_block = sinos[:, v0:v0 + vc, :N_DET].contiguous().cpu().pin_memory()
+        e2e_chunks = [B]
+
+        def e2e_call():
+            block[:, :, :N_DET].copy_(host_block, non_blocking=True)
+            fbp_step()
+            host_images.copy_(images, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+        h2d_bytes = B * vc * N_DET * 4 + vc * 8
+    else:
+        host_sinos = sinos[:, :, :N_DET].contiguous().cpu().pin_memory()
+        e2e_chunks = plan.host_chunks(B)
+
+        def e2e_call():
+            plan.run_batch_host(host_sinos, angles[0], host_images)
+        h2d_bytes = B * N_VIEW * N_DET * 4 + len(e2e_chunks) * N_VIEW * 8
+    e2e_call()
     barrier(world)
     e2e_steps = max(1, args.steps)
     t0 = time.perf_counter()
     for k in range(e2e_steps):
-        plan.run_batch_host(host_sinos, angles[0], host_images)
+        e2e_call()
     e2e_s = reduce_max(time.perf_counter() - t0, world)
     # parity spot check against the device path, and of the per-slice host call
     dev_imgs = images.cpu().numpy()
     e2e_err = float(np.linalg.norm(host_images.numpy() - dev_imgs) / np.linalg.norm(dev_imgs))
-    one = plan.run_host(host_sinos[B - 1].numpy(), angles[0])
-    single_err = float(np.linalg.norm(one - dev_imgs[B - 1]) / np.linalg.norm(dev_imgs[B - 1]))
+    single_err = None
+    if not shard_views:
+        one = plan.run_host(host_sinos[B - 1].numpy(), angles[0])
+        single_err = float(np.linalg.norm(one - dev_imgs[B - 1]) /
+                           np.linalg.norm(dev_imgs[B - 1]))
     # one slice through the single-slice entry point (the C++ Reconstructor's
     # and pjrec's call; device-resident sinogram), CUDA events
     one_img = torch.zeros((NX, NX), device="cuda")
@@ -694,14 +764,20 @@ def run_gpu(args):
     if rank != 0:
         return 0
     steps = args.steps
-    total_pv = PV_PER_SLICE * B * steps * world
+    # views: the ranks share the B slices (total work fixed); problems: each
+    # rank adds its own B slices
+    slices_total = B if shard_views else B * world
+    ray_world = 1 if shard_views else world   # views: every rank scans the same phantoms
+    total_pv = PV_PER_SLICE * slices_total * steps
     value = total_pv / (fbp_ms / 1e3)
     hbm, src, sm_mhz = peaks()
     sms = torch.cuda.get_device_properties(local).multi_processor_count
-    fp32_peak = sms * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    fp32_nominal = sms * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    fp32_peak = max(dev_peaks["ffma_tflops"], dev_peaks["ffma2_tflops"])
     bp_s = bp_avg_ms / 1e3
     flops = FLOP_PER_PV * PV_PER_SLICE * B
-    traffic = traffic_per_launch(B)
+    traffic, traffic_src = traffic_per_launch(B)
+    gather_gbs = BYTES_PER_PV * PV_PER_SLICE * B / bp_s / 1e9
     cpu_v, cpu_sample, cpu_threads = cpu_fbp_rate(seed=7, seconds=args.cpu_seconds,
                                                   views=args.ref_views)
     parity = oracle_parity(elems[0], elems[B - 1], g, sinos[B - 1], images[B - 1], angles[0])
@@ -709,22 +785,26 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": fbp_ms / steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "scaling": "strong" if shard_views else "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded random-ellipse phantoms, simulated on the device)",
         "config": {"workload": CONFIG_NAME, "batch_slices_per_step": B,
                    "l2": "inputs larger than L2 (%d sinograms x 2.1 MB + %d images x 1 MB)" % (B, B),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
-        "raysums": {"metric": "ray-sums/s", "value": RAYS_PER_SLICE * B * steps * world / (ray_ms / 1e3),
+                   "parallelism": ("view blocks of %d slices over %d GPUs, NCCL image sum in "
+                                   "the step" % (B, world)) if shard_views else
+                                  ("%d slices per GPU, contiguous ranges of a batch of %d, "
+                                   "no exchange" % (B, B * world)) if world > 1 else
+                                  "single GPU"},
+        "raysums": {"metric": "ray-sums/s", "value": RAYS_PER_SLICE * B * steps * ray_world / (ray_ms / 1e3),
                     "ms_per_step": ray_ms / steps,
-                    "ray_element_pairs_per_s": RAYS_PER_SLICE * 12 * B * steps * world / (ray_ms / 1e3),
+                    "ray_element_pairs_per_s": RAYS_PER_SLICE * 12 * B * steps * ray_world / (ray_ms / 1e3),
                     "launch": "all %d phantoms in one launch" % B,
                     # nominal 60 FLOP per ray-element pair (box test, two affine
                     # maps, circle clip with its square root, back-map and length)
                     "roofline": {"bound": "fp32 issue", "flop_per_pair": 60,
-                                 "achieved": RAYS_PER_SLICE * 12 * B * steps * world * 60 /
+                                 "achieved": RAYS_PER_SLICE * 12 * B * steps * ray_world * 60 /
                                              (ray_ms / 1e3) / 1e12,
                                  "peak": fp32_peak, "unit": "TFLOP/s",
-                                 "frac": RAYS_PER_SLICE * 12 * B * steps * world * 60 /
+                                 "frac": RAYS_PER_SLICE * 12 * B * steps * ray_world * 60 /
                                          (ray_ms / 1e3) / 1e12 / fp32_peak,
                                  "note": "set-up and ray kernels together; ncu: ray kernel "
                                          "issue slots ~89 % busy, set-up FP64 pipe ~70 % busy "
@@ -735,32 +815,38 @@ def run_gpu(args):
         "roofline": {"kernel": "backproject_table_kernel<equiangular,cubic>", "bound": "fp32",
                      "achieved": flops / bp_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": flops / bp_s / 1e12 / fp32_peak,
-                     "peak_source": "nominal FP32 of %d SMs x %d lanes x 2 FLOP x %.0f MHz "
-                                    "(max SM clock); MEASURED_PEAKS.json holds no FP32 figure"
-                                    % (sms, FP32_LANES_PER_SM, sm_mhz),
-                     "traffic": traffic,
+                     "peak_source": "measured in-run (packed FFMA2 microkernel, the higher of "
+                                    "FFMA2 %.1f and FFMA %.1f TFLOP/s); nominal %.1f TFLOP/s "
+                                    "(%d SMs x %d lanes x 2 FLOP x %.0f MHz)"
+                                    % (dev_peaks["ffma2_tflops"], dev_peaks["ffma_tflops"],
+                                       fp32_nominal, sms, FP32_LANES_PER_SM, sm_mhz),
+                     "frac_of_nominal": flops / bp_s / 1e12 / fp32_nominal,
+                     "traffic": traffic, "traffic_source": traffic_src,
                      "algorithmic_flops_per_launch": flops, "flop_per_pixel_view": FLOP_PER_PV,
                      "avg_launch_ms": bp_avg_ms, "slices_per_launch": B,
                      "hbm": {"achieved_gbs": traffic / bp_s / 1e9 if traffic else None,
                              "peak_gbs": hbm, "peak_source": src,
                              "frac": traffic / bp_s / 1e9 / hbm if traffic else None},
                      "gather": {"bytes_per_pixel_view": BYTES_PER_PV,
-                                "achieved_gbs": BYTES_PER_PV * PV_PER_SLICE * B / bp_s / 1e9,
+                                "achieved_gbs": gather_gbs,
                                 "served_from": "shared memory (rows staged by bulk copies)",
-                                "peak_gbs": sms * 128 * sm_mhz * 1e6 / 1e9,
-                                "peak_source": "nominal shared-memory bandwidth, %d SMs x 128 B "
-                                               "per clock x %.0f MHz; no measured figure"
-                                               % (sms, sm_mhz),
-                                "frac": BYTES_PER_PV * PV_PER_SLICE * B / bp_s / 1e9 /
-                                        (sms * 128 * sm_mhz * 1e6 / 1e9)}},
+                                "l2_gather16_peak_gbs": dev_peaks["l2_gather16_gbs"],
+                                "frac_of_l2_gather": gather_gbs / dev_peaks["l2_gather16_gbs"],
+                                "lds128_peak_gbs": dev_peaks["lds128_gbs"],
+                                "frac_of_lds128": gather_gbs / dev_peaks["lds128_gbs"],
+                                "l2_read_peak_gbs": dev_peaks["l2_read_gbs"],
+                                "peak_source": "measured in-run"},
+                     "device_peaks": dev_peaks},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                          "sample": cpu_sample},
         "parity_vs_fp64_oracle": parity,
-        "e2e": {"value": PV_PER_SLICE * B * e2e_steps * world / e2e_s, "unit": UNIT,
-                "h2d_bytes_per_step": B * N_VIEW * N_DET * 4 + len(e2e_chunks) * N_VIEW * 8,
-                "d2h_bytes_per_step": B * NX * NX * 4,
+        "e2e": {"value": PV_PER_SLICE * slices_total * e2e_steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": h2d_bytes * world,
+                "d2h_bytes_per_step": B * NX * NX * 4 * world,
                 "steps": e2e_steps, "ms_per_step": e2e_s / e2e_steps * 1e3,
-                "path": "ctgpu_recon_run_batch_host (page-locked host buffers, chunks of "
+                "path": ("view-sharded step with page-locked host blocks in and images out "
+                         "(sharding.reconstruct_views_batch's calls)") if shard_views else
+                        "ctgpu_recon_run_batch_host (page-locked host buffers, chunks of "
                         "%s slices, copies overlapped with compute)" % "+".join(map(str, e2e_chunks)),
                 "parity_vs_device_rel_l2": e2e_err,
                 "single_slice_run_host_rel_l2": single_err},
@@ -788,6 +874,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--shard", default="problems", choices=["problems", "views"],
+                    help="with several GPUs: each rank its own slices of a global batch "
+                         "(problems, weak scaling) or every rank a view block of the same "
+                         "slices with the images summed in the step (views, strong scaling)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--helical", type=int, default=1,

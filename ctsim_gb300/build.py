@@ -19,6 +19,9 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libctgpu.so")
 TOOL = os.path.join(PKG, "ctgpu_ctsimtext")
+# roofline denominators measured by the benchmark (FP32 FMA, shared-memory and
+# L2 gather bandwidth); not part of libctgpu
+PEAKS_LIB = os.path.join(PKG, "libctpeaks.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code keeps the reference's FP64 rounding: no contraction into FMAs
@@ -38,6 +41,7 @@ LIB_SOURCES = ["k_common.cu", "k_raysum.cu", "k_filter.cu", "k_backproject.cu", 
                "ctgpu_api.cpp", "filter_design.cpp", "ctsim_api.cpp", "k_noalloc.cu", "k_rebin.cu",
                "k_fileio.cu", "ctgpu_io.cpp", "k_fourier.cu", "ctgpu_fourier.cpp"]
 TOOL_SOURCES = ["tools/ctsimtext.cpp"]
+PEAKS_SOURCES = ["peaks/k_peaks.cu"]
 
 
 def nvcc():
@@ -76,8 +80,9 @@ def build(force=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     srcs = [os.path.join(CSRC, s) for s in LIB_SOURCES]
     tool_srcs = [os.path.join(CSRC, s) for s in TOOL_SOURCES]
+    peak_srcs = [os.path.join(CSRC, s) for s in PEAKS_SOURCES]
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
-        results = list(ex.map(lambda s: _compile(s, force), srcs + tool_srcs))
+        results = list(ex.map(lambda s: _compile(s, force), srcs + tool_srcs + peak_srcs))
     errs = [e for _, e in results if e]
     if errs:
         raise RuntimeError("compilation failed:\n" + "\n".join(errs))
@@ -85,7 +90,12 @@ def build(force=False, verbose=False):
     if force or _stale(LIB, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         subprocess.run(cmd, check=True)
-    tobjs = [o for o, _ in results[len(srcs):]]
+    nt = len(srcs) + len(tool_srcs)
+    tobjs = [o for o, _ in results[len(srcs):nt]]
+    pobjs = [o for o, _ in results[nt:]]
+    if pobjs and (force or _stale(PEAKS_LIB, pobjs)):
+        subprocess.run([nvcc()] + ARCH + ["-shared", "-o", PEAKS_LIB] + pobjs + ["-lcudart"],
+                       check=True)
     if tobjs and (force or _stale(TOOL, tobjs + [LIB])):
         cmd = [nvcc()] + ARCH + ["-o", TOOL] + tobjs + ["-L" + PKG, "-lctgpu", "-lcudart",
                                                        "-Xlinker", "-rpath=$ORIGIN"]
