@@ -6,9 +6,10 @@
 //
 //   ref_harness filter  GEOM NDET NVIEW DETINC FL SDL FILTER PARAM METHOD ZEROPAD GEN INTERPF in.f32 out.f64
 //       ProcessSignal::filterSignal on every row  (libctsim/procsignal.cpp:543)
-//   ref_harness bp      PJFILE filtered.f64 NX NY BACKPROJ INTERP out.f64
+//   ref_harness bp      PJFILE filtered.f64 NX NY BACKPROJ INTERP out.f64 [XMIN YMIN XMAX YMAX]
 //       Backprojector::BackprojectView per view + PostProcessing
-//       (libctsim/backprojectors.cpp:109-121)
+//       (libctsim/backprojectors.cpp:109-121), optionally with a
+//       ReconstructionROI (:284-315)
 //   ref_harness timerec PJFILE NX NY FILTER METHOD BACKPROJ INTERP NTHREADS [NVIEWS [PARAM [ZEROPAD]]]
 //       times Reconstructor over the first NVIEWS views, split across NTHREADS
 //       threads the way the GUI's worker threads do (one Reconstructor and one
@@ -68,7 +69,15 @@ static int cmdFilter(int argc, char** argv) {
 }
 
 static int cmdBackproject(int argc, char** argv) {
-  if (argc != 9) { fprintf(stderr, "bp: bad args\n"); return 2; }
+  if (argc != 9 && argc != 13) { fprintf(stderr, "bp: bad args\n"); return 2; }
+  ReconstructionROI roi;
+  const bool haveRoi = argc == 13;
+  if (haveRoi) {
+    roi.m_dXMin = atof(argv[9]);
+    roi.m_dYMin = atof(argv[10]);
+    roi.m_dXMax = atof(argv[11]);
+    roi.m_dYMax = atof(argv[12]);
+  }
   Projections pj;
   if (!pj.read(argv[2])) { fprintf(stderr, "pj read fail\n"); return 2; }
   int nx = atoi(argv[4]), ny = atoi(argv[5]);
@@ -76,7 +85,7 @@ static int cmdBackproject(int argc, char** argv) {
   std::vector<double> filt((size_t)nView * nDet);
   if (!readRaw(argv[3], filt.data(), filt.size() * 8)) { fprintf(stderr, "read fail\n"); return 2; }
   ImageFile im(nx, ny);
-  Backprojector bp(pj, im, argv[6], argv[7], 1, NULL);
+  Backprojector bp(pj, im, argv[6], argv[7], 1, haveRoi ? &roi : NULL);
   if (bp.fail()) { fprintf(stderr, "Backprojector: %s\n", bp.failMessage().c_str()); return 3; }
   for (int v = 0; v < nView; v++)
     bp.BackprojectView(&filt[(size_t)v * nDet], pj.getDetectorArray(v).viewAngle());

@@ -284,6 +284,42 @@ def make_phmfile(tmp):
     np.savez_compressed(os.path.join(HERE, "phmfile.npz"), **out)
 
 
+# reconstructions restricted to a region of interest (Backproject's
+# ReconstructionROI, libctsim/backprojectors.cpp:284-315; reachable through the
+# API, not pjrec): the reference's filtered rows (abs_bandlimit, convolution)
+# backprojected by the FP64-image build with the ROI
+ROIS = [  # (scan, nx, ny, backproj, interp, (xmin, ymin, xmax, ymax))
+    ("herman_par", 40, 36, "table", "linear", (-0.3, -0.45, 0.5, 0.35)),
+    ("herman_par", 33, 40, "idiff", "cubic", (-0.3, -0.45, 0.5, 0.35)),
+    ("herman_par", 40, 40, "diff", "nearest", (0.6, -0.2, -0.4, 0.5)),
+    ("herman_par", 40, 40, "trig", "linear", (0.6, -0.2, -0.4, 0.5)),
+    ("shepp_eqa", 36, 36, "table", "cubic", (-0.3, -0.45, 0.5, 0.35)),
+    ("herman_eql", 36, 30, "table", "linear", (-5.0, -0.4, 0.3, 5.0)),
+]
+
+
+def make_roi(tmp):
+    out = {}
+    harn64 = os.path.join(ROOT, "oracle", "_ref", "ref_harness64")
+    for k, (name, nx, ny, bp, ip, roi) in enumerate(ROIS):
+        pjf = os.path.join(tmp, name + ".pj")
+        sc = [x for x in SCANS if x[0] == name][0]
+        run(REF, "phm2pj", pjf, sc[3], sc[4], "--phantom", sc[1], "--geometry", sc[2],
+            "--nray", sc[5], *sc[6])
+        pj = read_pj(pjf)
+        fin, ff = os.path.join(tmp, "s.f32"), os.path.join(tmp, "f.f64")
+        np.ascontiguousarray(pj.data, np.float32).tofile(fin)
+        run(HARN, "filter", pj.geometry, pj.nDet, pj.nView, repr(pj.detInc), repr(pj.focalLength),
+            repr(pj.sourceDetectorLength), "abs_bandlimit", "-1", "convolution", 1, "direct", 1,
+            fin, ff)
+        fo = os.path.join(tmp, "img.f64")
+        run(harn64, "bp", pjf, ff, nx, ny, bp, ip, fo, *[repr(v) for v in roi])
+        out["%d/image64" % k] = np.fromfile(fo).reshape(nx, ny)
+        out["%d/cfg" % k] = np.array([name, nx, ny, bp, ip], dtype=object)
+        out["%d/roi" % k] = np.array(roi, np.float64)
+    np.savez_compressed(os.path.join(HERE, "roi.npz"), **out)
+
+
 def main():
     for b in (REF, REF64, HARN):
         if not os.path.exists(b):
@@ -306,6 +342,8 @@ def main():
             make_polar(tmp)
         if not only or "phmfile" in only:
             make_phmfile(tmp)
+        if not only or "roi" in only:
+            make_roi(tmp)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print("%-14s %8d bytes" % (f, os.path.getsize(os.path.join(HERE, f))))

@@ -30,34 +30,46 @@ def phantom_image(oracle, gaussian_filter, seed=4):
     return gaussian_filter(img, 1.0)
 
 
-def test_projector_dot_product(setup):
+def _smooth_sino(torch, op, oracle, gf, g, ang, seed):
+    """a structured sinogram: the FP64 projection of a smoothed phantom image"""
+    og = oracle.Geom(0, 733, 720, g.rot_inc, g.det_inc, g.focal_length,
+                     g.source_detector_length, g.view_diameter, 0.0)
+    s64 = oracle.project_image(og, phantom_image(oracle, gf, seed=seed), ang) * op.scale
+    s = torch.zeros_like(op.new_sino())
+    s[:, :733] = torch.from_numpy(s64.astype(np.float32)).cuda()
+    return s
+
+
+def test_projector_dot_product(setup, oracle):
+    """<P x, y> = <x, P^T y> to 1e-6 of <P x, y>, with x a smoothed phantom
+    image and y the projection of another one (so that the inner product is
+    not a small difference of large terms)."""
     torch, cg, ag, op, g, ang, gf = setup
-    torch.manual_seed(1)
-    x = torch.randn((512, 512), device="cuda", requires_grad=True)
-    y = torch.zeros_like(op.new_sino())
-    y[:, :733] = torch.randn((720, 733), device="cuda")
+    x = torch.from_numpy(phantom_image(oracle, gf, seed=6).astype(np.float32)).cuda()
+    x.requires_grad_(True)
+    y = _smooth_sino(torch, op, oracle, gf, g, ang, seed=7)
     px = ag.project(x, op)
     (gx,) = torch.autograd.grad((px * y).sum(), x)
-    lhs = float((px.double() * y.double()).sum())
+    lhs = float((px.detach().double() * y.double()).sum())
     rhs = float((x.detach().double() * gx.double()).sum())
-    # <Ax, y> = <x, A^T y>, relative to the Cauchy-Schwarz scale |Ax| |y|
-    scale = float(px.double().norm() * y.double().norm())
-    assert abs(lhs - rhs) <= 1e-6 * scale, (lhs, rhs, scale)
+    print("projector dot product: <Px,y> %.9g, <x,P^T y> %.9g, rel %.3g"
+          % (lhs, rhs, abs(lhs - rhs) / abs(lhs)))
+    assert abs(lhs - rhs) <= 1e-6 * abs(lhs), (lhs, rhs)
 
 
-def test_fbp_dot_product(setup):
+def test_fbp_dot_product(setup, oracle):
+    """<FBP s, w> = <s, FBP^T w> to 1e-6 of <FBP s, w>, with s the projection
+    of a smoothed phantom and w another smoothed phantom image."""
     torch, cg, ag, op, g, ang, gf = setup
-    torch.manual_seed(2)
-    s = torch.zeros_like(op.new_sino())
-    s[:, :733] = torch.randn((720, 733), device="cuda")
-    s.requires_grad_(True)
-    w = torch.randn((512, 512), device="cuda")
+    s = _smooth_sino(torch, op, oracle, gf, g, ang, seed=8).requires_grad_(True)
+    w = torch.from_numpy(phantom_image(oracle, gf, seed=10).astype(np.float32)).cuda()
     f = ag.fbp(s, op)
     (gs,) = torch.autograd.grad((f * w).sum(), s)
-    lhs = float((f.double() * w.double()).sum())
+    lhs = float((f.detach().double() * w.double()).sum())
     rhs = float((s.detach().double() * gs.double()).sum())
-    scale = float(f.double().norm() * w.double().norm())
-    assert abs(lhs - rhs) <= 1e-6 * scale, (lhs, rhs, scale)
+    print("FBP dot product: <FBP s,w> %.9g, <s,FBP^T w> %.9g, rel %.3g"
+          % (lhs, rhs, abs(lhs - rhs) / abs(lhs)))
+    assert abs(lhs - rhs) <= 1e-6 * abs(lhs), (lhs, rhs)
 
 
 def test_projection_loss_gradient(setup, oracle):
@@ -94,22 +106,49 @@ def test_projection_loss_gradient(setup, oracle):
 
 
 def test_fbp_loss_gradient(setup, oracle):
+    """d||FBP(s) - x_ref||^2 / ds against the FP64 reference gradient
+    2 F^T (rotScale B^T (FBP64(s) - x_ref)) -- the oracle's FP64
+    backprojection and its transpose, the reference's convolution filter in
+    FP64 (F^T from the reversed taps, so F's symmetry is not assumed) -- to
+    1e-5 rel-L2, and against central finite differences (h = 1e-3)."""
     torch, cg, ag, op, g, ang, gf = setup
-    x_ref = torch.from_numpy(phantom_image(oracle, gf).astype(np.float32)).cuda()
+    x_np = phantom_image(oracle, gf)
+    x_ref = torch.from_numpy(x_np.astype(np.float32)).cuda()
     torch.manual_seed(5)
     s = torch.zeros_like(op.new_sino())
     s[:, :733] = torch.rand((720, 733), device="cuda")
     s.requires_grad_(True)
     loss = ((ag.fbp(s, op) - x_ref) ** 2).sum()
     (gs,) = torch.autograd.grad(loss, s)
+
+    # FP64 reference gradient
+    og = oracle.Geom(0, 733, 720, g.rot_inc, g.det_inc, g.focal_length,
+                     g.source_detector_length, g.view_diameter, 0.0)
+    ps = oracle.ProcessSignal("abs_bandlimit", "convolution", 733, g.det_inc)
+    h = ps.filter_array()
+    n = 733
+
+    def conv_rows(a, taps):   # out[i] = detInc sum_j a[j] taps[i - j + n - 1]
+        return np.stack([g.det_inc * np.convolve(r, taps)[n - 1:2 * n - 1] for r in a])
+    s64 = s.detach()[:, :n].cpu().double().numpy()
+    rot = np.pi / 720
+    fbp64 = oracle.backproject(og, conv_rows(s64, h), ang, 512, 512, "table", "linear",
+                               post_process=True)
+    r64 = fbp64 - x_np.astype(np.float32).astype(np.float64)
+    g64 = 2 * rot * conv_rows(oracle.project_image(og, r64, ang), h[::-1])
+    e = rel_l2(gs[:, :n].cpu().numpy(), g64)
+    print("FBP loss gradient vs FP64 reference: rel-L2 %.3g" % e)
+    assert e < 1e-5, e
+    assert float(gs[:, n:].abs().max()) == 0.0
+
     d = torch.zeros_like(s)
     d[:, :733] = torch.randint(0, 2, (720, 733), device="cuda").float() * 2 - 1
-    h = 1e-3
+    hh = 1e-3
 
     def L(z):
         r = ag.fbp(z, op) - x_ref
         return float((r.double() ** 2).sum())
-    fd = (L(s.detach() + h * d) - L(s.detach() - h * d)) / (2 * h)
+    fd = (L(s.detach() + hh * d) - L(s.detach() - hh * d)) / (2 * hh)
     an = float((gs.double() * d.double()).sum())
     assert abs(fd - an) <= 1e-3 * abs(an) + 1e-6, (fd, an)
 

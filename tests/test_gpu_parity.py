@@ -468,3 +468,29 @@ def test_rasterize_matches_reference(gpu, golden):
         assert np.abs(a - ref64).max() <= 1e-6 * max(np.abs(ref64).max(), 1e-30)
         k += 1
     assert k == 3
+
+
+def test_roi_reconstructions_match_reference(gpu, golden):
+    """A plan with a region of interest (ctgpu_recon_create's roi,
+    ReconstructionROI of libctsim/backprojectors.cpp:284-315; a swapped and a
+    clamped ROI among them) against the reference's FP64 image of the same
+    ROI, rel-L2 <= 1e-5."""
+    torch, cg, device = gpu
+    scans = golden("scans")
+    d = golden("roi")
+    k = 0
+    while "%d/cfg" % k in d:
+        name, nx, ny, bp, ip = d["%d/cfg" % k]
+        nx, ny = int(nx), int(ny)
+        g = geom_from_hdr(cg, scans[name + "/hdr"])
+        plan = device.ReconPlan(g, nx, ny, "abs_bandlimit", -1.0, "convolution", 1, "direct", ip,
+                                1, bp, roi=tuple(d["%d/roi" % k]))
+        img = torch.zeros((nx, ny), device="cuda")
+        plan.run(to_dev(torch, device, scans[name + "/data"]), scans[name + "/angles"], img)
+        cg.sync()
+        ref = d["%d/image64" % k]
+        e = rel_l2(img.cpu().numpy(), ref)
+        print("ROI %s %s/%s: rel-L2 %.3g" % (name, bp, ip, e))
+        assert e < TOL, (d["%d/cfg" % k], e)
+        k += 1
+    assert k == 6
