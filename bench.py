@@ -270,15 +270,18 @@ def batched_uneven(args, torch, cg, device, phantoms, rank):
     rng = np.random.default_rng(2024 + rank)
     geos = ("parallel", "equiangular", "equilinear")
     probs, total_pv = [], 0
+    scans = []
     for i in range(args.batched_problems):
         side = int(rng.choice([128, 256, 512, 1024]))
         nv = int(rng.integers(180, 1441))
         nd = int(round(1.4 * side))
         geo = geos[int(rng.integers(0, 3))]
-        ph = phantoms.make_phantom(phantoms.random_ellipses(seed=i, n=int(rng.integers(5, 21))))
+        n_el = int(rng.integers(5, 21))
+        ph = phantoms.make_phantom(phantoms.random_ellipses(seed=i, n=n_el))
         sc = cg.Scanner(ph, geo, nd, nv)
         sino = device.alloc_sinogram(nv, nd)
         ang = device.raysums(sc, ph, sino)
+        scans.append((sc, ph, sino, nd * nv, nd * nv * n_el))
         probs.append(dict(geometry=sc.geometry(), nx=side, ny=side, sino=sino, angles=ang,
                           image=torch.zeros((side, side), device="cuda"),
                           filter_name="abs_hamming", filter_param=0.54, filter_method="fft",
@@ -312,7 +315,30 @@ def batched_uneven(args, torch, cg, device, phantoms, rank):
     cg.sync()
     seq_ms = s0.elapsed_time(s1)
     bps, cv = batch.shape()
+    # the same 64 scans in one set-up and one ray launch, against the
+    # per-problem sinograms made above
+    msinos = [torch.empty_like(q[2]) for q in scans]
+    device.raysums_multi([q[0] for q in scans], [q[1] for q in scans], msinos)
+    torch.cuda.synchronize()
+    same = all(torch.equal(m[:, :q[0].geometry().n_det], q[2][:, :q[0].geometry().n_det])
+               for m, q in zip(msinos, scans))
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    for _ in range(args.steps):
+        device.raysums_multi([q[0] for q in scans], [q[1] for q in scans], msinos)
+    r1.record(stream)
+    torch.cuda.synchronize()
+    cg.sync()
+    ray_ms = r0.elapsed_time(r1) / args.steps
+    rays = sum(q[3] for q in scans)
+    pairs = sum(q[4] for q in scans)
     return {"metric": METRIC, "value": total_pv / (ms / 1e3), "unit": UNIT,
+            "raysums": {"ms_per_run": ray_ms, "ray_sums": rays,
+                        "ray_sums_per_s": rays / (ray_ms / 1e3),
+                        "ray_element_pairs_per_s": pairs / (ray_ms / 1e3),
+                        "launch": "ctgpu_collect_projections_multi: every problem's scan in one "
+                                  "set-up and one ray launch (host records staged in one copy)",
+                        "equal_to_per_problem_scans": bool(same)},
             "ms_per_run": ms, "problems": len(probs), "pixel_view_updates_per_run": total_pv,
             "sides": sorted({q["nx"] for q in probs}),
             "launch": "one persistent backprojection launch + per-problem filter / set-up "
@@ -650,14 +676,10 @@ def run_gpu(args):
             for b in range(B):
                 plan.postprocess(images[b])
             return
-        # one filter launch for the batch's B x n_view rows, then the batch's
-        # backprojection (interval rows, tile records, backprojection)
-        plan.filter(sinos.view(B * N_VIEW, pitch), filtered.view(B * N_VIEW, pitch))
-        if bp_events is not None:
-            bp_events[0].record(stream)
-        plan.backproject_batch(filtered, angles[0], images)
-        if bp_events is not None:
-            bp_events[1].record(stream)
+        # ctgpu_recon_run_batch: one filter launch for the batch's B x n_view
+        # rows, which also writes the interval rows; the tile records; one
+        # backprojection launch for the B slices
+        plan.run_batch(sinos, angles[0], images)
 
     for _ in range(max(args.warmup, 1)):
         raysum_step()
@@ -683,8 +705,27 @@ def run_gpu(args):
     barrier(world)
     cg.sync()
     fbp_ms = reduce_max(e0.elapsed_time(e1), world)
-    bp_ms = [s.elapsed_time(e) for (s, e) in bp_ev]
-    bp_avg_ms = float(np.mean(bp_ms))       # one launch = B slices
+    if shard_views:
+        bp_avg_ms = float(np.mean([s.elapsed_time(e) for (s, e) in bp_ev]))
+        filt_avg_ms = None
+    else:
+        # the step's kernels apart, CUDA events on the launching stream: the
+        # filter launch over B x n_view rows, and the batched backprojection
+        # (its tile records, and here its own interval-row pass, then the main
+        # kernel; the ncu launch list gives the main kernel's share)
+        fe = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        for k in range(args.steps):
+            fe[k][0].record(stream)
+            plan.filter(sinos.view(B * N_VIEW, pitch), filtered.view(B * N_VIEW, pitch))
+            fe[k][1].record(stream)
+            bp_ev[k][0].record(stream)
+            plan.backproject_batch(filtered, angles[0], images)
+            bp_ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        cg.sync()
+        filt_avg_ms = float(np.mean([s.elapsed_time(e) for (s, e) in fe]))
+        bp_avg_ms = float(np.mean([s.elapsed_time(e) for (s, e) in bp_ev]))
 
     # --- timed: ray-sums -----------------------------------------------------------
     r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -854,7 +895,20 @@ def run_gpu(args):
         # backprojection itself for the batch
         "single_slice": {"ms": single_ms, "value": PV_PER_SLICE / (single_ms / 1e3), "unit": UNIT,
                          "call": "ctgpu_recon_run (one slice, its views in groups of blocks)"},
-        "gpu_launches": steps * 4,
+        # per step: filter (rows fused), tile records, backprojection; sharded
+        # by views: filter, interval rows, tile records, backprojection and B
+        # PostProcessing launches
+        "gpu_launches": steps * ((4 + B) if shard_views else 3),
+        "filter": None if filt_avg_ms is None else {
+            "kernel": "fft_filter_persistent_kernel<11>", "avg_launch_ms": filt_avg_ms,
+            "rows_per_launch": B * N_VIEW,
+            "algorithmic_bytes_per_launch": B * N_VIEW * N_DET * 8,
+            "achieved_gbs": B * N_VIEW * N_DET * 8 / (filt_avg_ms / 1e3) / 1e9,
+            "frac_hbm": B * N_VIEW * N_DET * 8 / (filt_avg_ms / 1e3) / 1e9 / hbm,
+            # the survey's FFT-filter constant per view: 2 x 2.5 N log2 N + 6 N
+            "flop_per_launch": B * N_VIEW * (2 * 2.5 * 2048 * 11 + 6 * 2048),
+            "note": "two views per complex transform of length 2048; the launch of "
+                    "ctgpu_recon_run_batch also writes the 16-byte interval rows"},
         "batched_uneven": batched,
         "helical": helical,
         "files": files,

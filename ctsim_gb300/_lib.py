@@ -93,6 +93,7 @@ SIGNATURES = {
     "ctgpu_scanner_geometry": ([_p, C.POINTER(Geometry)], _i),
     "ctgpu_collect_projections": ([_p, _p, _i, _i, _i, _i, _p, _i, _p, _p], _i),
     "ctgpu_collect_projections_batch": ([_p, _pp, _i, _p, _i, C.c_longlong, _p, _p], _i),
+    "ctgpu_collect_projections_multi": ([_pp, _pp, _i, _pp, _p, _pp, _p], _i),
     "ctgpu_collect_projections_host": ([_p, _p, _i, _i, _i, _i, _p, _p], _i),
     "ctgpu_scanner_destroy": ([_p], None),
     "ctgpu_recon_create": ([C.POINTER(Geometry), _i, _i, _s, _d, _s, _i, _s, _s, _i, _s,

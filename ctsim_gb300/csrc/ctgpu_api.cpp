@@ -853,6 +853,101 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   return ok();
 }
 
+int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
+                                    const ctgpu_phantom* const* phantoms, int n,
+                                    float* const* d_sinos, const int* pitches,
+                                    double* const* h_angles, void* stream) {
+  if (!scanners || !phantoms || !d_sinos || !pitches || n < 1)
+    return fail(CTGPU_ERR_INVALID, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  // one staging copy: per problem [ray records][parallel directions][elements],
+  // then the problems' launch descriptors and the two block-offset tables
+  struct Part { size_t oV, oD, oE, oRec; };
+  std::vector<Part> parts(n);
+  size_t total = 0;
+  for (int k = 0; k < n; k++) {
+    ctgpu_scanner* s = scanners[k];
+    const ctgpu_phantom* p = phantoms[k];
+    if (!s || !p || !d_sinos[k]) return fail(CTGPU_ERR_INVALID, "null scanner, phantom or sinogram");
+    if (pitches[k] < s->nDet) return fail(CTGPU_ERR_INVALID, "sinogram pitch smaller than nDet");
+    if (p->unitPulse) return fail(CTGPU_ERR_UNSUPPORTED, "unit-pulse phantoms are not batched");
+    if (p->elems.empty()) return fail(CTGPU_ERR_INVALID, "phantom has no elements");
+    scanner_views(s, 0, s->nView, 0);
+    if (h_angles && h_angles[k])
+      for (int v = 0; v < s->nView; v++) h_angles[k][v] = s->views[v].angle;
+    CUDA_TRY(ensure_arc_table(s));
+    parts[k].oV = total;
+    total = up16(total + sizeof(RayView) * s->nView);
+    parts[k].oD = total;
+    if (s->geometry == kParallel) total = up16(total + sizeof(float2) * s->nView * s->nSample);
+    parts[k].oE = total;
+    total = up16(total + sizeof(PElem) * p->elems.size());
+  }
+  const size_t oP = total;
+  total = up16(total + sizeof(RaysumLaunch) * n);
+  const size_t oS = total;
+  total = up16(total + sizeof(int) * (n + 1));
+  const size_t oR = total;
+  total = up16(total + sizeof(int) * (n + 1));
+  ctgpu_scanner* s0 = scanners[0];
+  // device buffers first: the descriptors point into them
+  CUDA_TRY(ensure_device(s0->d_stage, s0->d_stage_cap, total));
+  unsigned char* h = nullptr;
+  int slot = 0;
+  CUDA_TRY(stage_host(s0, total, &h, &slot));
+  std::vector<RaysumLaunch> L(n);
+  std::vector<int> setupStart(n + 1, 0), rayStart(n + 1, 0);
+  size_t smem = 0, recBytes = 0;
+  for (int k = 0; k < n; k++) {
+    ctgpu_scanner* s = scanners[k];
+    const ctgpu_phantom* p = phantoms[k];
+    const int nv = s->nView;
+    stage_ray_views(s, nv, h + parts[k].oV, parts[k].oD - parts[k].oV);
+    std::memcpy(h + parts[k].oE, p->elems.data(), sizeof(PElem) * p->elems.size());
+    RaysumLaunch& q = L[k];
+    q = RaysumLaunch{};
+    q.geometry = s->geometry;
+    q.nDet = s->nDet;
+    q.nSample = s->nSample;
+    q.nElem = (int)p->elems.size();
+    q.nViews = nv;
+    q.pitch = pitches[k];
+    q.rowOffset = 0;
+    q.centerDetectorLength = s->centerDetectorLength;
+    q.angularDetLen = s->angularDetLen;
+    q.angularDetInc = s->angularDetInc;
+    q.elems = reinterpret_cast<const PElem*>(s0->d_stage + parts[k].oE);
+    q.views = reinterpret_cast<const RayView*>(s0->d_stage + parts[k].oV);
+    q.sdirs = s->geometry == kParallel
+                  ? reinterpret_cast<const float2*>(s0->d_stage + parts[k].oD) : nullptr;
+    q.arc = s->d_arc;
+    q.arcHalf = s->d_half;
+    q.sino = d_sinos[k];
+    q.status = status_pointer();
+    q.nSlices = 1;
+    const size_t sm = raysum_prepare(q);
+    if (sm > smem) smem = sm;
+    parts[k].oRec = recBytes;
+    recBytes = (recBytes + raysum_record_bytes(q, q.nElem) + 255) & ~(size_t)255;
+    setupStart[k + 1] = setupStart[k] + raysum_setup_blocks(q);
+    rayStart[k + 1] = rayStart[k] + nv;
+  }
+  CUDA_TRY(ensure_device(s0->d_records, s0->d_records_cap, recBytes));
+  for (int k = 0; k < n; k++) L[k].records = s0->d_records + parts[k].oRec;
+  std::memcpy(h + oP, L.data(), sizeof(RaysumLaunch) * n);
+  std::memcpy(h + oS, setupStart.data(), sizeof(int) * (n + 1));
+  std::memcpy(h + oR, rayStart.data(), sizeof(int) * (n + 1));
+  CUDA_TRY(stage_send(s0, slot, total, st));
+  cudaError_t e = launch_raysum_multi(reinterpret_cast<const RaysumLaunch*>(s0->d_stage + oP),
+                                      reinterpret_cast<const int*>(s0->d_stage + oS),
+                                      setupStart[n], reinterpret_cast<const int*>(s0->d_stage + oR),
+                                      rayStart[n], n, smem, st);
+  if (e == cudaErrorInvalidValue)
+    return fail(CTGPU_ERR_UNSUPPORTED, "too many phantom elements x rays per detector for one CTA");
+  CUDA_TRY(e);
+  return ok();
+}
+
 int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ell, int n, double z0,
                                          double dz, float* d_sino, int pitch, double* h_angles,
                                          void* stream) {
@@ -1131,11 +1226,26 @@ void ctgpu_recon_destroy(ctgpu_recon* r) { delete r; }
 // Filtering of nBatch sinograms of nViews rows each, one launch.
 // narrowOk: a launch of few blocks may use the N / 8-thread transform (the
 // single-slice entry point; batched launches keep one arithmetic)
+// Where a filter launch may also write the interval rows of the table-family
+// backprojection that follows it (FilterLaunch::rows).
+struct RowsTarget {
+  void* rows = nullptr;
+  int interp = 0, pitch = 0;
+  size_t sliceStride = 0;
+};
+
 static int recon_filter_batch(ctgpu_recon* r, const float* d_sino, int sinoPitch,
                               size_t sinoStride, int nViews, float* d_filtered, int filtPitch,
                               size_t filtStride, int nBatch, cudaStream_t st,
-                              bool narrowOk = false) {
+                              bool narrowOk = false, const RowsTarget* rows = nullptr,
+                              bool* rowsWritten = nullptr) {
   FilterLaunch L{};
+  if (rows) {
+    L.rows = rows->rows;
+    L.rowsInterp = rows->interp;
+    L.rowsPitch = rows->pitch;
+    L.rowsSliceStride = rows->sliceStride;
+  }
   L.narrowOk = narrowOk ? 1 : 0;
   L.nDet = r->g.n_det;
   L.nViews = nViews;
@@ -1150,7 +1260,7 @@ static int recon_filter_batch(ctgpu_recon* r, const float* d_sino, int sinoPitch
   L.nBatch = nBatch;
   L.inSliceStride = sinoStride;
   L.outSliceStride = filtStride;
-  cudaError_t e = launch_filter(L, st);
+  cudaError_t e = launch_filter(L, st, rowsWritten);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "nDet too large for the shared-memory FFT filter (at most 8192)");
   CUDA_TRY(e);
@@ -1234,7 +1344,7 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
                                     const unsigned char* reuseScratch = nullptr,
                                     bool anglesOnDevice = false,
                                     unsigned char* extScratch = nullptr,
-                                    bool splitViews = false) {
+                                    bool splitViews = false, bool rowsReady = false) {
   if (nViews <= 0) {
     if (!accumulate)
       for (int b = 0; b < nBatch; b++)
@@ -1293,6 +1403,7 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
   }
   L.reuseRecords = reuseScratch && reuseScratch == scratch && stable && r->bproj != kDiff &&
                    r->bproj != kIDiff;
+  L.rowsReady = rowsReady ? 1 : 0;
   cudaError_t e = launch_backproject_views(L, views, scratch, st);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "image pixels behind the fan-beam source");
@@ -1423,15 +1534,39 @@ static int recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int
     CUDA_TRY(ensure_device(r->d_filtered, r->d_filtered_cap, fStride * nBatch));
     filtered = r->d_filtered;
   }
+  // The table family's scratch (records, then interval rows) comes first, so
+  // that the filter launch can write the rows from its own output and the
+  // backprojection skips its row pass.
+  unsigned char* scratch = bufs ? bufs->scratch : nullptr;
+  RowsTarget rt;
+  if (r->bproj != kDiff && r->bproj != kIDiff) {
+    BackprojLaunch L = make_launch(r, nView, r->pitch, nullptr, filtered, d_images, 0, 1.f,
+                                   nBatch, fStride, (size_t)imageSliceStride);
+    size_t off = 0;
+    if (table_rows_layout(L, &off, &rt.pitch, &rt.interp)) {
+      if (!scratch) {
+        const size_t sb = backproject_scratch_bytes(L);
+        const size_t capBefore = r->d_scratch_cap;
+        CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
+        // a reallocated scratch holds no records for reuseScratch
+        if (r->d_scratch_cap != capBefore) reuseScratch = nullptr;
+        scratch = r->d_scratch;
+      }
+      rt.rows = scratch + off;
+      rt.sliceStride = (size_t)nView * rt.pitch;
+    }
+  }
+  bool rowsWritten = false;
   int rc = recon_filter_batch(r, d_sinos, sinoPitch, (size_t)sinoSliceStride, nView,
-                              filtered, r->pitch, fStride, nBatch, st);
+                              filtered, r->pitch, fStride, nBatch, st, false,
+                              rt.rows ? &rt : nullptr, &rowsWritten);
   if (rc) return rc;
   float scale = raw_scale(r);
   bool post = (flags & CTGPU_RUN_POSTPROCESS) != 0;
   if (post && r->bproj != kTrig) scale = (float)(scale * r->rotScale);
   return recon_backproject_scaled(r, filtered, r->pitch, h_angles, nView, d_images, 0, scale,
                                   st, nBatch, fStride, (size_t)imageSliceStride, reuseScratch,
-                                  anglesOnDevice, bufs ? bufs->scratch : nullptr);
+                                  anglesOnDevice, scratch, false, rowsWritten);
 }
 
 // Chunk sizes of a host-buffer batch.  Consecutive chunks run on two compute
@@ -2127,11 +2262,20 @@ static int batch_enqueue_prep(ctgpu_batch* b, cudaStream_t s) {
   for (size_t i = 0; i < b->probs.size(); i++) {
     BatchEntry& e = b->probs[i];
     cudaStream_t ss = b->side[i % kSideStreams];
+    // the filter writes the problem's interval rows too, where its kernel can
+    RowsTarget rt;
+    rt.rows = b->d_arena + e.scratchOff + e.prep.recBytes;
+    rt.interp = e.L.interp;
+    rt.pitch = e.prep.rpitch;
+    rt.sliceStride = (size_t)e.L.nViews * e.prep.rpitch;
+    bool rowsWritten = false;
     int rc = recon_filter_batch(e.plan, e.d_sino, e.sinoPitch, 0, e.L.nViews,
                                 reinterpret_cast<float*>(b->d_arena + e.filtOff), e.plan->pitch,
-                                0, 1, ss);
+                                0, 1, ss, false, &rt, &rowsWritten);
     if (rc) return rc;
-    CUDA_TRY(launch_table_prep(e.L, e.prep, b->d_arena + e.scratchOff, ss));
+    BackprojLaunch Lp = e.L;
+    Lp.rowsReady = rowsWritten ? 1 : 0;
+    CUDA_TRY(launch_table_prep(Lp, e.prep, b->d_arena + e.scratchOff, ss));
   }
   for (int k = 0; k < kSideStreams; k++) {
     CUDA_TRY(cudaEventRecord(b->join[k], b->side[k]));

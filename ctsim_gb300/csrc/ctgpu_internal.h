@@ -106,7 +106,18 @@ struct FilterLaunch {
   // a launch of few blocks may give each transform N / 8 threads (the
   // single-slice entry points; batched launches keep one arithmetic)
   int narrowOk;
+  // optional: the table-family backprojection's interval rows of the filtered
+  // views (k_backproject.cu's layout: kRowPad zero elements before sample 0,
+  // rowsPitch elements per view, rowsSliceStride elements between slices),
+  // written by the filter kernel from its output when rows != null and the
+  // kernel chosen can (launch_filter reports it)
+  void* rows;
+  int rowsInterp;
+  int rowsPitch;
+  size_t rowsSliceStride;
 };
+// zero row elements before sample 0 of an interval row
+constexpr int kRowPad = 4;
 
 // Backprojection of one problem.
 struct BackprojLaunch {
@@ -132,6 +143,9 @@ struct BackprojLaunch {
   // [viewGroups][nx][ny] (set by the launch, in the set-up scratch)
   int viewGroups;
   float* partial;
+  // table family: the interval rows in scratch were written by the filter
+  // launch ordered before this one (launch_filter's rows)
+  int rowsReady;
 };
 
 struct HelicalLaunch {
@@ -230,9 +244,20 @@ cudaError_t launch_raysum_ellipse_grad(const RaysumLaunch& L, const float* gsino
                                        cudaStream_t s);
 // scratch of launch_raysum: one record per (phantom, view, element, ray sample)
 size_t raysum_record_bytes(const RaysumLaunch& L, int totalElems);
+// Many scans (each its own geometry, detectors, views and phantom) in one
+// set-up and one ray launch.  raysum_prepare completes a descriptor (1/CD,
+// the arctangent table) and returns its ray blocks' shared memory;
+// raysum_setup_blocks gives its set-up blocks.  d_probs: the n descriptors in
+// device memory; d_setupStart / d_rayStart: n + 1 block offsets each.
+size_t raysum_prepare(RaysumLaunch& L);
+int raysum_setup_blocks(const RaysumLaunch& L);
+cudaError_t launch_raysum_multi(const RaysumLaunch* d_probs, const int* d_setupStart,
+                                int setupBlocks, const int* d_rayStart, int rayBlocks, int n,
+                                size_t smem, cudaStream_t s);
 cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int rowOffset,
                               cudaStream_t s);
-cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s);
+// *rowsWritten (if given): whether the launch also wrote L.rows
+cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s, bool* rowsWritten = nullptr);
 size_t backproject_scratch_bytes(const BackprojLaunch& L);
 // blocks of the table-family main kernel resident per SM (its occupancy target)
 int backproject_table_ctas_per_sm();
@@ -251,6 +276,9 @@ struct TablePrep {
   size_t recBytes, rowBytes;   // scratch: the records, then the rows
 };
 bool table_prep_info(const BackprojLaunch& L, TablePrep* out);
+// where a table-family launch keeps its interval rows in scratch: byte offset,
+// elements per view and the interpolation; false for other backprojectors
+bool table_rows_layout(const BackprojLaunch& L, size_t* offsetBytes, int* rpitch, int* interp);
 // interval rows and (tile, view) records of one problem into scratch
 cudaError_t launch_table_prep(const BackprojLaunch& L, const TablePrep& P, void* scratch,
                               cudaStream_t s);

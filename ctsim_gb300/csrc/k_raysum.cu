@@ -411,16 +411,15 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
 // active or all, so the set-up runs apart from the rays in full warps.
 // Records of phantom z start at elemOffset[z] * nViews * nSub.
 template <int GEOM>
-__global__ void __launch_bounds__(128) raysum_setup_kernel(RaysumLaunch L) {
+__device__ __forceinline__ void setup_block(const RaysumLaunch& L, int bx, int z) {
   const int nSub = (GEOM == kParallel) ? L.nSample : 1;
-  const int z = blockIdx.y;
   int off = 0, nElem = L.nElem;
   if (L.elemOffset) {
     off = L.elemOffset[z];
     nElem = L.elemOffset[z + 1] - off;
   }
   const int per = nElem * nSub;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int idx = bx * blockDim.x + threadIdx.x;
   if (idx >= L.nViews * per) return;
   const int view = idx / per, ks = idx % per;
   ElemView* rec = static_cast<ElemView*>(L.records) + (size_t)off * L.nViews * nSub;
@@ -429,17 +428,21 @@ __global__ void __launch_bounds__(128) raysum_setup_kernel(RaysumLaunch L) {
 }
 
 template <int GEOM>
-__global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
-  extern __shared__ __align__(16) ElemView ev[];
-  const int view = blockIdx.x;
+__global__ void __launch_bounds__(128) raysum_setup_kernel(RaysumLaunch L) {
+  setup_block<GEOM>(L, blockIdx.x, blockIdx.y);
+}
+
+// One view of one phantom's sinogram (ev: the block's shared memory).
+template <int GEOM>
+__device__ __forceinline__ void ray_block(const RaysumLaunch& L, int view, int z, ElemView* ev) {
   const int nS = L.nSample;
   const int nSub = (GEOM == kParallel) ? nS : 1;
   const PElem* elems = L.elems;
   int off = 0, nElem = L.nElem;
-  float* sino = L.sino + (size_t)blockIdx.y * L.sliceStride;
+  float* sino = L.sino + (size_t)z * L.sliceStride;
   if (L.elemOffset) {
-    off = L.elemOffset[blockIdx.y];
-    nElem = L.elemOffset[blockIdx.y + 1] - off;
+    off = L.elemOffset[z];
+    nElem = L.elemOffset[z + 1] - off;
     elems += off;
   }
   if (L.elemsPerView) elems += (size_t)view * nElem;
@@ -577,6 +580,53 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
   }
 }
 
+template <int GEOM>
+__global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
+  extern __shared__ __align__(16) ElemView ev[];
+  ray_block<GEOM>(L, blockIdx.x, blockIdx.y, ev);
+}
+
+// Many scans in one launch each: problem k's descriptor is probs[k] (in
+// device memory), and its blocks are blockStart[k] .. blockStart[k+1) of the
+// grid (setup: records / 128; rays: one block per view).
+__device__ __forceinline__ int problem_of_block(const int* __restrict__ blockStart, int n) {
+  int lo = 0, hi = n - 1;
+  const int b = blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (blockStart[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(128) raysum_setup_multi_kernel(const RaysumLaunch* __restrict__ probs,
+                                                                 const int* __restrict__ blockStart,
+                                                                 int n) {
+  const int k = problem_of_block(blockStart, n);
+  const RaysumLaunch& L = probs[k];
+  const int bx = blockIdx.x - blockStart[k];
+  switch (L.geometry) {
+    case kParallel: setup_block<kParallel>(L, bx, 0); break;
+    case kEquilinear: setup_block<kEquilinear>(L, bx, 0); break;
+    default: setup_block<kEquiangular>(L, bx, 0); break;
+  }
+}
+
+__global__ void __launch_bounds__(128, 4) raysum_multi_kernel(const RaysumLaunch* __restrict__ probs,
+                                                           const int* __restrict__ blockStart,
+                                                           int n) {
+  extern __shared__ __align__(16) ElemView ev[];
+  const int k = problem_of_block(blockStart, n);
+  const RaysumLaunch& L = probs[k];
+  const int view = blockIdx.x - blockStart[k];
+  switch (L.geometry) {
+    case kParallel: ray_block<kParallel>(L, view, 0, ev); break;
+    case kEquilinear: ray_block<kEquilinear>(L, view, 0, ev); break;
+    default: ray_block<kEquiangular>(L, view, 0, ev); break;
+  }
+}
+
 __global__ void unit_pulse_kernel(float* sino, int nViews, int nDet, int pitch, int rowOffset) {
   int v = blockIdx.x;
   for (int d = threadIdx.x; d < nDet; d += blockDim.x)
@@ -623,6 +673,35 @@ cudaError_t launch_raysum(const RaysumLaunch& L0, cudaStream_t s) {
     case kEquilinear: return raysum_launch<kEquilinear>(L, smem, nSlices, s);
     default: return raysum_launch<kEquiangular>(L, smem, nSlices, s);
   }
+}
+
+size_t raysum_prepare(RaysumLaunch& L) {
+  L.invCD = L.centerDetectorLength != 0.0 ? 1.0 / L.centerDetectorLength : 0.0;
+  std::copy(atan64_table().v, atan64_table().v + 65, L.atan64);
+  const int nSub = (L.geometry == kParallel) ? L.nSample : 1;
+  return dir_table_offset((L.nElem > 0 ? L.nElem : 1) * nSub) +
+         sizeof(float2) * (size_t)L.nSample;
+}
+
+int raysum_setup_blocks(const RaysumLaunch& L) {
+  const int nSub = (L.geometry == kParallel) ? L.nSample : 1;
+  return (L.nViews * L.nElem * nSub + 127) / 128;
+}
+
+cudaError_t launch_raysum_multi(const RaysumLaunch* d_probs, const int* d_setupStart,
+                                int setupBlocks, const int* d_rayStart, int rayBlocks, int n,
+                                size_t smem, cudaStream_t s) {
+  if (n <= 0 || rayBlocks <= 0) return cudaSuccess;
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  if (setupBlocks > 0)
+    raysum_setup_multi_kernel<<<setupBlocks, 128, 0, s>>>(d_probs, d_setupStart, n);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(raysum_multi_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  raysum_multi_kernel<<<rayBlocks, 128, smem, s>>>(d_probs, d_rayStart, n);
+  return cudaGetLastError();
 }
 
 __global__ void ellipsoid_section_kernel(const PElem* base, const double2* zc, int n, int nViews,

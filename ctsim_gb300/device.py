@@ -75,6 +75,32 @@ def raysums_batch(scanner, phantoms, sinos, stream=None):
     return ang
 
 
+def raysums_multi(scanners, phantoms, sinos, stream=None):
+    """collectProjections of many (scanner, phantom) problems of different
+    geometry, detectors and views in one set-up and one ray launch
+    (ctgpu_collect_projections_multi): sinos[k] a device [n_view_k, pitch_k]
+    tensor; returns the view angles of every problem."""
+    n = len(scanners)
+    if len(phantoms) != n or len(sinos) != n:
+        raise ValueError("one phantom and one sinogram per scanner")
+    geos = [sc.geometry() for sc in scanners]
+    for g, t in zip(geos, sinos):
+        if t.shape[0] < g.n_view or t.shape[1] < g.n_det:
+            raise ValueError("sinogram smaller than its scan")
+    angs = [np.zeros(g.n_view, np.float64) for g in geos]
+
+    def hv(x):
+        return x.value if hasattr(x, "value") else x
+    sh = (C.c_void_p * n)(*[hv(sc._h) for sc in scanners])
+    ph = (C.c_void_p * n)(*[hv(p._h) for p in phantoms])
+    sp = (C.c_void_p * n)(*[_ptr(t).value for t in sinos])
+    pitches = (C.c_int * n)(*[t.shape[1] for t in sinos])
+    ap = (C.c_void_p * n)(*[a.ctypes.data for a in angs])
+    check(lib().ctgpu_collect_projections_multi(sh, ph, n, sp, pitches, ap,
+                                                stream_handle(stream)))
+    return angs
+
+
 class ReconPlan:
     """A Reconstructor for device tensors (ctgpu_recon)."""
 

@@ -135,6 +135,19 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
                                     int n_phantoms, float* d_sinos, int sino_pitch,
                                     long long sino_slice_stride, double* h_view_angles,
                                     void* stream);
+/* Many scans of uneven shapes in one set-up launch and one ray launch: problem
+ * k scans phantoms[k] with scanners[k] (each its own geometry, nDet, nView
+ * and nSample) over all its views into d_sinos[k] (rows of sino_pitches[k]
+ * floats) and, if h_view_angles and h_view_angles[k] are not NULL, stores its
+ * view angles there.  Each sinogram is what ctgpu_collect_projections writes
+ * for the problem alone.  No reference counterpart as one call: the reference
+ * scans one phantom per Scanner::collectProjections
+ * (libctsim/scanner.cpp:280-419).  The scanners[0]'s staging and record
+ * buffers carry the launch; unit-pulse phantoms are not batched. */
+int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
+                                    const ctgpu_phantom* const* phantoms, int n,
+                                    float* const* d_sinos, const int* sino_pitches,
+                                    double* const* h_view_angles, void* stream);
 /* Helical scan of a 3-D phantom of n_ellipsoids ellipsoids, all n_view views
  * of the scanner (its geometry is that of a 2-D phantom; make it from the
  * ellipsoids' largest cross-sections).  View v sees the phantom's

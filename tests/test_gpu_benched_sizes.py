@@ -10,9 +10,10 @@
   slice positions through one helical plan; the FBP of all 64 slices at
   1024 x 1024 (Shepp by FFT, zero-pad 2, linear) as one ctgpu_batch.  The
   first, a middle and the last slice are checked.
-- The main workload's timed sequence: one filter launch over B x 720 rows,
-  then one batched backprojection of the B slices (equiangular 733 x 720,
-  12 ellipses, 512 x 512, cubic), B = 3.
+- The main workload's timed step, ctgpu_recon_run_batch: one filter launch
+  over B x 720 rows (which also writes the interval rows), then one batched
+  backprojection of the B slices (equiangular 733 x 720, 12 ellipses,
+  512 x 512, cubic), B = 3.
 
 Tolerances: rel-L2 <= 1e-5 against FP64 for sinograms and images (the path's
 precision bar).  The z-interpolated rows, fed the same FP32 scan as the
@@ -140,8 +141,9 @@ def test_helical_workload_full_size(gpu, oracle):
 
 
 def test_bench_timed_sequence(gpu, oracle):
-    """plan.filter over the batch's B x 720 rows in one launch, then
-    plan.backproject_batch, as the benchmark's timed step does."""
+    """plan.run_batch over the batch's B slices (one filter launch over the
+    B x 720 rows that also writes the interval rows, then one backprojection
+    launch), as the benchmark's timed step does."""
     torch, cg, device, phantoms = gpu
     po = oracle
     B, nd, nv, nx = 3, 733, 720, 512
@@ -151,13 +153,11 @@ def test_bench_timed_sequence(gpu, oracle):
     g = sc.geometry()
     pitch = device.pitch_for(nd)
     sinos = torch.zeros((B, nv, pitch), device="cuda")
-    filtered = torch.zeros((B, nv, pitch), device="cuda")
     images = torch.full((B, nx, nx), float("nan"), device="cuda")
     plan = device.ReconPlan(g, nx, nx, "abs_hamming", 0.54, "fft", 2, "direct", "cubic", 1,
                             "table")
     ang = device.raysums_batch(sc, phs, sinos)
-    plan.filter(sinos.view(B * nv, pitch), filtered.view(B * nv, pitch))
-    plan.backproject_batch(filtered, ang, images)
+    plan.run_batch(sinos, ang, images)
     cg.sync()
     osc = po.Scanner(po.Phantom(elements=elems[0]), "equiangular", nd, nv, nsample=1)
     for b in range(B):
