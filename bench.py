@@ -794,6 +794,15 @@ def run_gpu(args):
     torch.cuda.synchronize()
     cg.sync()
     single_ms = s0.elapsed_time(s1) / max(args.steps, 1)
+    # the same slice end to end through ctgpu_recon_run_host (pjrec's and the
+    # C++ Reconstructor's host-buffer call): sinogram up, image back, per call
+    host_one = np.ascontiguousarray(sinos[0, :, :N_DET].cpu().numpy())
+    plan.run_host(host_one, angles[0])
+    reps = max(args.steps, 5)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        plan.run_host(host_one, angles[0])
+    single_host_ms = (time.perf_counter() - t0) / reps * 1e3
 
     batched = batched_uneven(args, torch, cg, device, phantoms, rank) \
         if args.batched_problems > 0 else None
@@ -894,7 +903,13 @@ def run_gpu(args):
         # per step: one filter launch; interval rows, tile records and the
         # backprojection itself for the batch
         "single_slice": {"ms": single_ms, "value": PV_PER_SLICE / (single_ms / 1e3), "unit": UNIT,
-                         "call": "ctgpu_recon_run (one slice, its views in groups of blocks)"},
+                         "call": "ctgpu_recon_run (one slice, its views in groups of blocks)",
+                         "e2e": {"value": PV_PER_SLICE / (single_host_ms / 1e3), "unit": UNIT,
+                                 "ms": single_host_ms,
+                                 "h2d_bytes_per_call": N_VIEW * N_DET * 4 + N_VIEW * 8,
+                                 "d2h_bytes_per_call": NX * NX * 4,
+                                 "call": "ctgpu_recon_run_host (pageable numpy buffers, "
+                                         "synchronous)"}},
         # per step: filter (rows fused), tile records, backprojection; sharded
         # by views: filter, interval rows, tile records, backprojection and B
         # PostProcessing launches
