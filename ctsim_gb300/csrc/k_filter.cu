@@ -20,8 +20,10 @@
 // Two kernels:
 //   fft_filter_persistent_kernel (batched launches, fftN 512 .. 4096): a
 //     persistent grid, each block looping over view pairs with its twiddle
-//     factors held in registers; it can also write the interval rows of the
-//     table-family backprojection straight from its output;
+//     factors held in registers and the next pair's rows on their way into
+//     shared memory (cp.async) while it transforms the current one; it can
+//     also write the interval rows of the table-family backprojection straight
+//     from its output;
 //   fft_filter_kernel (one CTA per view pair and slice; the single-slice
 //     launches of few blocks, and fftN 8192 and 16384, whose sequences
 //     need dynamic shared memory): k_fft.cuh's shared-memory
@@ -153,23 +155,89 @@ __device__ __forceinline__ void run_passes(float2* buf, const float2 (&twr)[NT])
 
 // 512 / T blocks of T threads: at most 128 registers, which hold the
 // twiddles (27-38 complex values) and one butterfly without spilling
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc, unsigned bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 template <int LOG2N>
 __global__ void __launch_bounds__((1 << LOG2N) / 16, 512 / ((1 << LOG2N) / 16))
     fft_filter_persistent_kernel(FilterLaunch L, int vec) {
   constexpr int N = 1 << LOG2N, T = N / 16, NQ = N / 4 / T;   // quads per thread (4)
   constexpr int NT = PassInfo<N, 1>::TOTAL;
+  // a row has n <= N/2 samples, so only a thread's first JP quads can hold
+  // samples; with 16-byte rows, each thread copies those quads of the next
+  // pair into its own slots of stg while the current pair is transformed
+  constexpr int JP = 2;
+  constexpr bool PREF = LOG2N <= 11;   // stg fits the 48 KB of static shared memory
   __shared__ __align__(16) float2 zb[N + N / 16];
+  __shared__ __align__(16) float4 stg[PREF ? 2 * JP * T : 1];
   float2 twr[NT > 0 ? NT : 1];
   load_pass_twiddles<N, 1, 0>(twr, L.twiddle);
   const int n = L.nDet;
   const int pairs = (L.nViews + 1) / 2;
   const long long units = (long long)pairs * L.nBatch;
+  const bool pref = PREF && vec;
+  float4 wr[JP];
+#pragma unroll
+  for (int j = 0; j < JP; j++) {
+    const int m = 4 * (threadIdx.x + j * T);
+    float t[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) t[e] = m + e < n ? __ldg(&L.weights[m + e]) : 0.f;
+    wr[j] = make_float4(t[0], t[1], t[2], t[3]);
+  }
+  auto prefetch = [&](long long uu) {
+    const int z = (int)(uu / pairs), pr = (int)(uu - (long long)z * pairs);
+    const int v0 = 2 * pr;
+    const bool two = v0 + 1 < L.nViews;
+    const float* ia = L.in + (size_t)z * L.inSliceStride + (size_t)v0 * L.inPitch;
+    const float* ib = ia + L.inPitch;
+#pragma unroll
+    for (int j = 0; j < JP; j++) {
+      const int m = 4 * (threadIdx.x + j * T);
+      const int rem = n - m;
+      const unsigned bytes = rem >= 4 ? 16u : rem > 0 ? 4u * rem : 0u;
+      cp_async16(&stg[j * T + threadIdx.x], bytes ? ia + m : ia, bytes);
+      cp_async16(&stg[(JP + j) * T + threadIdx.x], (two && bytes) ? ib + m : ia,
+                 two ? bytes : 0u);
+    }
+    cp_async_commit();
+  };
+  if (pref && blockIdx.x < units) prefetch(blockIdx.x);
   for (long long u = blockIdx.x; u < units; u += gridDim.x) {
     const int z = (int)(u / pairs), pr = (int)(u - (long long)z * pairs);
     const int v0 = 2 * pr;
     const bool two = v0 + 1 < L.nViews;
     const float* ia = L.in + (size_t)z * L.inSliceStride + (size_t)v0 * L.inPitch;
     const float* ib = two ? ia + L.inPitch : ia;
+    if (pref) {
+      // this pair's rows from the thread's own slots, weighted; then the
+      // next pair's copies go out
+      cp_async_wait_all();
+#pragma unroll
+      for (int j = 0; j < NQ; j++) {
+        const int m = 4 * (threadIdx.x + j * T);
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+        if (j < JP) {
+          const float4 w = wr[j < JP ? j : 0];
+          a = stg[j * T + threadIdx.x];
+          b = stg[(JP + j) * T + threadIdx.x];
+          a = make_float4(w.x * a.x, w.y * a.y, w.z * a.z, w.w * a.w);
+          b = make_float4(w.x * b.x, w.y * b.y, w.z * b.z, w.w * b.w);
+        }
+        float2* d = zb + pslot(m);
+        d[0] = make_float2(a.x, b.x);
+        d[1] = make_float2(a.y, b.y);
+        d[2] = make_float2(a.z, b.z);
+        d[3] = make_float2(a.w, b.w);
+      }
+      if (u + gridDim.x < units) prefetch(u + gridDim.x);
+    } else {
     // weighted rows a (real part) and b (imaginary part), zero padded to N
 #pragma unroll
     for (int j = 0; j < NQ; j++) {
@@ -201,6 +269,7 @@ __global__ void __launch_bounds__((1 << LOG2N) / 16, 512 / ((1 << LOG2N) / 16))
       d[1] = make_float2(a.y, b.y);
       d[2] = make_float2(a.z, b.z);
       d[3] = make_float2(a.w, b.w);
+    }
     }
     __syncthreads();
     run_passes<N, 1, 0>(zb, twr);
