@@ -238,6 +238,9 @@ def run_reference(args):
     return 0
 
 
+INSTR_PER_PV = [None]   # thread instructions per pixel-view update (ncu summary)
+
+
 def traffic_per_launch(batch):
     """DRAM bytes (read + write) of one backprojection launch of `batch` slices,
     from the committed ncu summary of the same kernel (captured at its own
@@ -248,13 +251,16 @@ def traffic_per_launch(batch):
     vals = {}
     with open(p) as f:
         for line in f:
-            for key in ("traffic_bytes_per_launch:", "traffic_batch_slices:", "captured_at_commit:"):
+            for key in ("traffic_bytes_per_launch:", "traffic_batch_slices:", "captured_at_commit:",
+                        "thread_instructions_per_update:"):
                 if line.startswith(key):
                     vals[key] = line.split(":", 1)[1].strip()
     if "traffic_bytes_per_launch:" not in vals or "traffic_batch_slices:" not in vals:
         return None, None
     src = "profiles/backproject_equiangular_cubic_512_ncu.md, captured at commit %s" % \
         vals.get("captured_at_commit:", "unknown")
+    INSTR_PER_PV[0] = float(vals["thread_instructions_per_update:"]) \
+        if "thread_instructions_per_update:" in vals else None
     return (float(vals["traffic_bytes_per_launch:"]) * batch /
             float(vals["traffic_batch_slices:"]), src)
 
@@ -886,6 +892,16 @@ def run_gpu(args):
                                 "frac_of_lds128": gather_gbs / dev_peaks["lds128_gbs"],
                                 "l2_read_peak_gbs": dev_peaks["l2_read_gbs"],
                                 "peak_source": "measured in-run"},
+                     # what the kernel executes: thread instructions per
+                     # update (the ncu summary) at the live launch time,
+                     # against 4 schedulers x 32 lanes per SM per cycle
+                     "issue": None if INSTR_PER_PV[0] is None else {
+                         "thread_instructions_per_update": INSTR_PER_PV[0],
+                         "achieved_tinst_per_s": INSTR_PER_PV[0] * PV_PER_SLICE * B / bp_s,
+                         "peak_tinst_per_s": sms * 4 * 32 * sm_mhz * 1e6,
+                         "frac": INSTR_PER_PV[0] * PV_PER_SLICE * B / bp_s /
+                                 (sms * 4 * 32 * sm_mhz * 1e6),
+                         "source": "instruction count from the profile's ncu capture"},
                      "device_peaks": dev_peaks},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                          "sample": cpu_sample},
