@@ -1451,6 +1451,7 @@ int ctgpu_recon_run(ctgpu_recon* r, const float* d_sino, int sinoPitch, const do
   // angles only, so they are built on a side stream while the filter runs;
   // the scratch is sized here as the backprojection below sizes it
   const unsigned char* recs = nullptr;
+  RowsTarget rt;
   if (nViews > 0 && r->bproj != kDiff && r->bproj != kIDiff) {
     CUDA_TRY(ensure_device(r->d_angles, r->d_angles_cap, (size_t)nViews));
     CUDA_TRY(cudaMemcpyAsync(r->d_angles, h_angles + startView, sizeof(double) * nViews,
@@ -1470,14 +1471,25 @@ int ctgpu_recon_run(ctgpu_recon* r, const float* d_sino, int sinoPitch, const do
     CUDA_TRY(e);
     CUDA_TRY(cudaEventRecord(r->sideEv[1], r->s_side));
     recs = r->d_scratch;
+    // the filter writes the interval rows after the records, in the same
+    // scratch (the records' set-up does not touch them)
+    size_t off = 0;
+    if (table_rows_layout(L, &off, &rt.pitch, &rt.interp)) {
+      rt.rows = r->d_scratch + off;
+      rt.sliceStride = (size_t)nViews * rt.pitch;
+    }
   }
-  int rc = ctgpu_recon_filter(r, d_sino + (size_t)startView * sinoPitch, sinoPitch, nViews,
-                              r->d_filtered, r->pitch, stream);
+  if (!d_sino) return fail(CTGPU_ERR_INVALID, "null argument");
+  if (sinoPitch < r->g.n_det) return fail(CTGPU_ERR_INVALID, "pitch < nDet");
+  bool rowsWritten = false;
+  int rc = recon_filter_batch(r, d_sino + (size_t)startView * sinoPitch, sinoPitch, 0, nViews,
+                              r->d_filtered, r->pitch, 0, 1, st, true, rt.rows ? &rt : nullptr,
+                              &rowsWritten);
   if (rc) return rc;
   if (recs) CUDA_TRY(cudaStreamWaitEvent(st, r->sideEv[1], 0));
   rc = recon_backproject_scaled(r, r->d_filtered, r->pitch, h_angles + startView, nViews, d_image,
                                 acc ? 1 : 0, scale, st, 1, 0, 0, recs, recs != nullptr, nullptr,
-                                true);
+                                true, rowsWritten);
   if (rc) return rc;
   if (post && acc) return ctgpu_recon_postprocess(r, d_image, stream);
   return ok();
@@ -1576,24 +1588,32 @@ static int recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int
 // chunk's output copy, a wait wherever a chunk's input copy outlasts the
 // previous chunk's compute, and the second-to-last chunk's output copy where it
 // outlasts the last chunk's compute.  A dynamic program over (slices covered,
-// last chunk size) minimises the sum, in milliseconds from rough GB300 rates
-// (1.1e12 pixel-view updates/s, 200 GB/s host to device, 180 GB/s back,
-// 10 us per chunk).  For 64 slices of 512^2 it picks 1 + 17 + 44 + 2.
-static std::vector<int> plan_chunks(int nBatch, int maxChunk, long long tilesPerSlice,
-                                    long long resident, double waveMs, double inMs, double outMs) {
-  const int S = std::min(maxChunk, nBatch);
-  auto comp = [&](int sz) { return (double)(tilesPerSlice * sz) / resident * waveMs + 0.01; };
+// last chunk size) minimises the sum, in milliseconds from GB300 rates
+// (1.35e12 pixel-view updates/s, 200 GB/s host to device, 180 GB/s back,
+// 30 us per chunk).  Chunks hold at least minChunk slices (a full wave of
+// tiles: smaller ones leave the SMs they cannot fill idle, e.g. 1 + 31 + 31
+// + 1 slices of 512^2 took 9.54 ms against 9.37 ms for 2 + 30 + 30 + 2) and
+// at most maxChunk (larger ones measured slower: 1 + 17 + 44 + 2 9.46 ms,
+// 64 10.06 ms, 4 + 28 + 28 + 4 9.34 ms).  For 64 slices of 512^2 it picks
+// 3 + 30 + 28 + 3.
+static std::vector<int> plan_chunks(int nBatch, int maxChunk, int minChunk,
+                                    long long tilesPerSlice, long long resident, double waveMs,
+                                    double inMs, double outMs) {
+  const int S = std::max(1, std::min(maxChunk, nBatch));
+  minChunk = std::max(1, std::min(minChunk, S));   // the staging cap comes first
+  if (nBatch <= minChunk) return std::vector<int>(1, nBatch);
+  auto comp = [&](int sz) { return (double)(tilesPerSlice * sz) / resident * waveMs + 0.03; };
   const double inf = 1e300;
   // f[i * (S + 1) + s]: the first i slices covered, the last chunk of size s
   std::vector<double> f((size_t)(nBatch + 1) * (S + 1), inf);
   std::vector<int> prev((size_t)(nBatch + 1) * (S + 1), 0);
   auto at = [&](int i, int sz) { return (size_t)i * (S + 1) + sz; };
-  for (int sz = 1; sz <= S; sz++) f[at(sz, sz)] = inMs * sz + comp(sz);
+  for (int sz = minChunk; sz <= S; sz++) f[at(sz, sz)] = inMs * sz + comp(sz);
   for (int i = 1; i < nBatch; i++)
     for (int sz = 1; sz <= std::min(S, i); sz++) {
       const double base = f[at(i, sz)];
       if (base >= inf) continue;
-      for (int s2 = 1; s2 <= std::min(S, nBatch - i); s2++) {
+      for (int s2 = minChunk; s2 <= std::min(S, nBatch - i); s2++) {
         const double c = base + comp(s2) + std::max(0.0, inMs * s2 - comp(sz));
         if (c < f[at(i + s2, s2)]) {
           f[at(i + s2, s2)] = c;
@@ -1602,7 +1622,7 @@ static std::vector<int> plan_chunks(int nBatch, int maxChunk, long long tilesPer
       }
     }
   double best = inf;
-  int last = 1;
+  int last = 0;
   for (int sz = 1; sz <= S; sz++) {
     if (f[at(nBatch, sz)] >= inf) continue;
     const int p = prev[at(nBatch, sz)];
@@ -1612,6 +1632,7 @@ static std::vector<int> plan_chunks(int nBatch, int maxChunk, long long tilesPer
       last = sz;
     }
   }
+  if (last == 0) return std::vector<int>(1, nBatch);   // no split obeys the bounds
   std::vector<int> sizes;
   for (int i = nBatch, sz = last; i > 0;) {
     sizes.push_back(sz);
@@ -1644,9 +1665,14 @@ static cudaError_t host_chunk_sizes(const ctgpu_recon* r, int nBatch, std::vecto
   const long long tilesPerSlice = (long long)((r->nx + kBackprojTile - 1) / kBackprojTile) *
                                   ((r->ny + kBackprojTile - 1) / kBackprojTile);
   const long long resident = (long long)sms * backproject_table_ctas_per_sm();
-  const double waveMs = (double)resident * kBackprojTile * kBackprojTile * nView / 1.1e9;
-  *sizes = plan_chunks(nBatch, maxChunk, tilesPerSlice, resident, waveMs,
-                       sizeof(float) * sStride / 2e8, sizeof(float) * iStride / 1.8e8);
+  const double waveMs = (double)resident * kBackprojTile * kBackprojTile * nView / 1.35e9;
+  // a chunk fills the resident blocks at least once and spans at most about
+  // 13 waves of them
+  const int minChunk = (int)std::max<long long>(1, (resident + tilesPerSlice - 1) / tilesPerSlice);
+  const int waveCap = (int)std::min<long long>(64, std::max<long long>(minChunk,
+                                                     13 * resident / tilesPerSlice));
+  *sizes = plan_chunks(nBatch, std::min(maxChunk, waveCap), minChunk, tilesPerSlice, resident,
+                       waveMs, sizeof(float) * sStride / 2e8, sizeof(float) * iStride / 1.8e8);
   r->plannedChunks = *sizes;
   r->plannedFor = nBatch;
   r->plannedDev = dev;

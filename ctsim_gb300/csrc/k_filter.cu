@@ -27,7 +27,7 @@
 //   fft_filter_kernel (one CTA per view pair and slice; the single-slice
 //     launches of few blocks, and fftN 8192 and 16384, whose sequences
 //     need dynamic shared memory): k_fft.cuh's shared-memory
-//     Stockham transform.
+//     Stockham transform; it writes the interval rows too where asked.
 #include <algorithm>
 #include <cstdint>
 
@@ -72,6 +72,33 @@ __global__ void __launch_bounds__(MAXT) fft_filter_kernel(FilterLaunch L) {
     const float2 y = zb[fpad<M>(m)];
     oa[m] = y.x;
     if (two) ob[m] = -y.y;
+  }
+  // the interval rows of both views, as the persistent kernel writes them
+  if (L.rows) {
+    const int rp = L.rowsPitch;
+    const size_t rbase = (size_t)blockIdx.y * L.rowsSliceStride + (size_t)v0 * rp;
+    const float2* zs = zb;
+    auto fa = [zs](int i) { return zs[fpad<M>(i)].x; };
+    auto fb = [zs](int i) { return -zs[fpad<M>(i)].y; };
+    if (L.rowsInterp == kCubic) {
+      float4* rr = static_cast<float4*>(L.rows) + rbase;
+      for (int j = threadIdx.x; j < rp; j += blockDim.x) {
+        rr[j] = interval_elem<kCubic>(fa, j - kRowPad, n);
+        if (two) rr[rp + j] = interval_elem<kCubic>(fb, j - kRowPad, n);
+      }
+    } else if (L.rowsInterp == kLinear) {
+      float2* rr = static_cast<float2*>(L.rows) + rbase;
+      for (int j = threadIdx.x; j < rp; j += blockDim.x) {
+        rr[j] = interval_elem<kLinear>(fa, j - kRowPad, n);
+        if (two) rr[rp + j] = interval_elem<kLinear>(fb, j - kRowPad, n);
+      }
+    } else {
+      float* rr = static_cast<float*>(L.rows) + rbase;
+      for (int j = threadIdx.x; j < rp; j += blockDim.x) {
+        rr[j] = interval_elem<kNearest>(fa, j - kRowPad, n);
+        if (two) rr[rp + j] = interval_elem<kNearest>(fb, j - kRowPad, n);
+      }
+    }
   }
 }
 
@@ -423,6 +450,7 @@ cudaError_t launch_filter(const FilterLaunch& L, cudaStream_t s, bool* rowsWritt
   }
   dim3 grid((L.nViews + 1) / 2, nBatch);
   kern<<<grid, T, smem, s>>>(L);
+  if (rowsWritten) *rowsWritten = L.rows != nullptr;
   return cudaGetLastError();
 }
 
