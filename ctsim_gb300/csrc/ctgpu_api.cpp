@@ -2203,10 +2203,11 @@ void ctgpu_helical_plan_destroy(ctgpu_helical_plan* p) { delete p; }
 
 // ---------------------------------------------------------------------------
 // Batched reconstruction of problems of uneven sizes.  Each problem keeps a
-// plan of its own (filter design, image grid, geometry); the set-up launches
-// of the problems (filter, interval rows, tile records) run as parallel
-// branches on kSideStreams streams, then one persistent launch backprojects
-// every (problem, tile) item, longest first.
+// plan of its own (filter design, image grid, geometry) and its (tile, view)
+// records, built once at create (the view angles are fixed there); at each
+// run the problems' filter launches, which write the interval rows too, run
+// as parallel branches on kSideStreams streams, then one persistent launch
+// backprojects every (problem, tile) item, longest first.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -2301,6 +2302,7 @@ static int batch_enqueue_prep(ctgpu_batch* b, cudaStream_t s) {
     if (rc) return rc;
     BackprojLaunch Lp = e.L;
     Lp.rowsReady = rowsWritten ? 1 : 0;
+    Lp.reuseRecords = 1;   // built at create
     CUDA_TRY(launch_table_prep(Lp, e.prep, b->d_arena + e.scratchOff, ss));
   }
   for (int k = 0; k < kSideStreams; k++) {
@@ -2415,7 +2417,11 @@ int ctgpu_batch_create(const ctgpu_batch_problem* problems, int n, int flags, ct
                         sizeof(double) * e.L.nViews, cudaMemcpyHostToDevice));
     const int tiles = ((e.L.nx + 31) / 32) * ((e.L.ny + 31) / 32);
     for (int t = 0; t < tiles; t++) b->items.push_back(BatchItem{i, t});
+    // the (tile, view) records depend on the geometry, the image grid and the
+    // view angles only, all fixed from here on: built once, kept in the arena
+    CUDA_TRY(launch_tile_setup(e.L, b->d_arena + e.scratchOff, nullptr));
   }
+  CUDA_TRY(cudaStreamSynchronize(nullptr));
   // longest first: a tile's cost is its problem's view count
   std::stable_sort(b->items.begin(), b->items.end(), [&](const BatchItem& x, const BatchItem& y) {
     return b->probs[x.problem].L.nViews > b->probs[y.problem].L.nViews;

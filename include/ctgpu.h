@@ -289,9 +289,11 @@ typedef struct {
 } ctgpu_batch_problem;
 #define CTGPU_BATCH_AUTOTUNE 1   /* time the launch shapes on the first run, keep the fastest */
 #define CTGPU_BATCH_GRAPH 2      /* capture the batch in a CUDA graph after the first run, replay it */
-/* Plans every problem (filters, windows, work list); diff / idiff are not
- * batched (CTGPU_ERR_UNSUPPORTED).  The buffers named by the problems must
- * stay valid while the batch is used. */
+/* Plans every problem (filters, windows, work list) and builds its
+ * backprojection's (tile, view) records, which depend on the geometry, the
+ * image grid and the view angles only; diff / idiff are not batched
+ * (CTGPU_ERR_UNSUPPORTED).  Synchronous.  The buffers named by the problems
+ * must stay valid while the batch is used. */
 int ctgpu_batch_create(const ctgpu_batch_problem* problems, int n_problems, int flags,
                        ctgpu_batch** out);
 /* Filters and backprojects every problem (PostProcessing included) on
