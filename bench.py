@@ -919,7 +919,8 @@ def run_gpu(args):
         # per step: one filter launch; interval rows, tile records and the
         # backprojection itself for the batch
         "single_slice": {"ms": single_ms, "value": PV_PER_SLICE / (single_ms / 1e3), "unit": UNIT,
-                         "call": "ctgpu_recon_run (one slice, its views in groups of blocks)",
+                         "call": "ctgpu_recon_run (one slice, its views in groups of blocks; "
+                                 "the same angles each call, so the plan keeps its tile records)",
                          "e2e": {"value": PV_PER_SLICE / (single_host_ms / 1e3), "unit": UNIT,
                                  "ms": single_host_ms,
                                  "h2d_bytes_per_call": N_VIEW * N_DET * 4 + N_VIEW * 8,

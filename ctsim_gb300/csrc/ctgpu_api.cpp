@@ -330,6 +330,11 @@ struct ctgpu_recon {
   // ctgpu_recon_run: the tile records' stream (beside the filter) and events
   cudaStream_t s_side = nullptr;
   cudaEvent_t sideEv[2] = {};
+  // the view angles whose (tile, view) records d_scratch holds, while
+  // recKeyValid: ctgpu_recon_run builds them only for other angles, and every
+  // other writer of d_scratch's records (or a reallocation) clears the key
+  std::vector<double> recKey;
+  bool recKeyValid = false;
   cudaEvent_t ev[6] = {};   // in_done[2], comp_done[2], out_done[2]
   double* h_angles_pinned = nullptr;   // page-locked copy of the view angles
   size_t h_angles_cap = 0;
@@ -1403,6 +1408,7 @@ static int recon_backproject_scaled(ctgpu_recon* r, const float* d_filtered, int
   }
   L.reuseRecords = reuseScratch && reuseScratch == scratch && stable && r->bproj != kDiff &&
                    r->bproj != kIDiff;
+  if (scratch == r->d_scratch && !L.reuseRecords) r->recKeyValid = false;   // rewritten below
   L.rowsReady = rowsReady ? 1 : 0;
   cudaError_t e = launch_backproject_views(L, views, scratch, st);
   if (e == cudaErrorInvalidValue)
@@ -1459,17 +1465,30 @@ int ctgpu_recon_run(ctgpu_recon* r, const float* d_sino, int sinoPitch, const do
     BackprojLaunch L = make_launch(r, nViews, r->pitch, r->d_angles, r->d_filtered, d_image,
                                    acc ? 1 : 0, scale, 1, 0, 0);
     CUDA_TRY(set_view_groups(r, L));
+    const size_t capBefore = r->d_scratch_cap;
     CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, backproject_scratch_bytes(L)));
+    if (r->d_scratch_cap != capBefore) r->recKeyValid = false;
     if (!r->s_side) CUDA_TRY(cudaStreamCreateWithFlags(&r->s_side, cudaStreamNonBlocking));
     for (cudaEvent_t& e : r->sideEv)
       if (!e) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    CUDA_TRY(cudaEventRecord(r->sideEv[0], st));   // angles up; the last call's work queued
-    CUDA_TRY(cudaStreamWaitEvent(r->s_side, r->sideEv[0], 0));
-    cudaError_t e = launch_tile_setup(L, r->d_scratch, r->s_side);
-    if (e == cudaErrorInvalidValue)
-      return fail(CTGPU_ERR_UNSUPPORTED, "image pixels behind the fan-beam source");
-    CUDA_TRY(e);
-    CUDA_TRY(cudaEventRecord(r->sideEv[1], r->s_side));
+    // records of the same angles (bit for bit) are still in the scratch when
+    // the last call built them and nothing has rewritten them since (slices
+    // of one scan reconstructed in turn)
+    const double* ang = h_angles + startView;
+    const bool have = r->recKeyValid && r->recKey.size() == (size_t)nViews &&
+                      std::memcmp(r->recKey.data(), ang, sizeof(double) * nViews) == 0;
+    if (!have) {
+      r->recKeyValid = false;
+      CUDA_TRY(cudaEventRecord(r->sideEv[0], st));   // angles up; the last call's work queued
+      CUDA_TRY(cudaStreamWaitEvent(r->s_side, r->sideEv[0], 0));
+      cudaError_t e = launch_tile_setup(L, r->d_scratch, r->s_side);
+      if (e == cudaErrorInvalidValue)
+        return fail(CTGPU_ERR_UNSUPPORTED, "image pixels behind the fan-beam source");
+      CUDA_TRY(e);
+      CUDA_TRY(cudaEventRecord(r->sideEv[1], r->s_side));
+      r->recKey.assign(ang, ang + nViews);
+      r->recKeyValid = true;
+    }
     recs = r->d_scratch;
     // the filter writes the interval rows after the records, in the same
     // scratch (the records' set-up does not touch them)
@@ -1560,6 +1579,7 @@ static int recon_run_batch(ctgpu_recon* r, int nBatch, const float* d_sinos, int
         const size_t sb = backproject_scratch_bytes(L);
         const size_t capBefore = r->d_scratch_cap;
         CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb));
+        r->recKeyValid = false;   // its records are rebuilt for this batch
         // a reallocated scratch holds no records for reuseScratch
         if (r->d_scratch_cap != capBefore) reuseScratch = nullptr;
         scratch = r->d_scratch;
@@ -1767,6 +1787,7 @@ int ctgpu_recon_run_batch_host(ctgpu_recon* r, int nBatch, const float* h_sinos,
                                    fStride, iStride);
     const size_t sb = backproject_scratch_bytes(L);
     CUDA_TRY(ensure_device(r->d_scratch, r->d_scratch_cap, sb ? sb : 1));
+    r->recKeyValid = false;   // the chunks rebuild its records
     if (sets > 1) CUDA_TRY(ensure_device(r->d_scratch2, r->d_scratch2_cap, sb ? sb : 1));
     bufs[0] = ChunkBufs{r->d_filtered, r->d_scratch};
     bufs[1] = ChunkBufs{r->d_filtered2, r->d_scratch2};
