@@ -321,7 +321,7 @@ def batched_uneven(args, torch, cg, device, phantoms, rank):
     cg.sync()
     seq_ms = s0.elapsed_time(s1)
     bps, cv = batch.shape()
-    # the same 64 scans in one set-up and one ray launch, against the
+    # the same 64 scans in one ray launch, against the
     # per-problem sinograms made above
     msinos = [torch.empty_like(q[2]) for q in scans]
     device.raysums_multi([q[0] for q in scans], [q[1] for q in scans], msinos)
@@ -343,7 +343,7 @@ def batched_uneven(args, torch, cg, device, phantoms, rank):
                         "ray_sums_per_s": rays / (ray_ms / 1e3),
                         "ray_element_pairs_per_s": pairs / (ray_ms / 1e3),
                         "launch": "ctgpu_collect_projections_multi: every problem's scan in one "
-                                  "set-up and one ray launch (host records staged in one copy)",
+                                  "ray launch (host records staged in one copy)",
                         "equal_to_per_problem_scans": bool(same)},
             "ms_per_run": ms, "problems": len(probs), "pixel_view_updates_per_run": total_pv,
             "sides": sorted({q["nx"] for q in probs}),

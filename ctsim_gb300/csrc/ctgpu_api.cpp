@@ -243,8 +243,6 @@ struct ctgpu_scanner {
   size_t d_views_cap = 0;
   float2* d_sdirs = nullptr;
   size_t d_sdirs_cap = 0;
-  unsigned char* d_records = nullptr;
-  size_t d_records_cap = 0;
   float* d_sino = nullptr;
   size_t d_sino_cap = 0;
   // collect_projections_ellipsoids: the ellipsoids' largest cross-sections,
@@ -283,7 +281,7 @@ struct ctgpu_scanner {
   std::vector<float2> h_dirs;
   ~ctgpu_scanner() {
     for (void* p : {(void*)d_views, (void*)d_sino, (void*)d_belems,
-                    (void*)d_sdirs, (void*)d_records, (void*)d_velems, (void*)d_zc,
+                    (void*)d_sdirs, (void*)d_velems, (void*)d_zc,
                     (void*)d_arc, (void*)d_half, (void*)d_stage})
       if (p) cudaFree(p);
     for (int b = 0; b < 2; b++) {
@@ -781,8 +779,6 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
   L.arcHalf = s->d_half;
   L.sino = d_sino;
   L.status = status_pointer();
-  CUDA_TRY(ensure_device(s->d_records, s->d_records_cap, raysum_record_bytes(L, L.nElem)));
-  L.records = s->d_records;
   cudaError_t e = launch_raysum(L, st);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "too many phantom elements x rays per detector for one CTA");
@@ -847,8 +843,6 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   L.nSlices = n;
   L.elemOffset = reinterpret_cast<const int*>(s->d_stage + oO);
   L.sliceStride = (size_t)sliceStride;
-  CUDA_TRY(ensure_device(s->d_records, s->d_records_cap, raysum_record_bytes(L, (int)all.size())));
-  L.records = s->d_records;
   cudaError_t e = launch_raysum(L, st);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "too many phantom elements x rays per detector for one CTA");
@@ -866,8 +860,8 @@ int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
     return fail(CTGPU_ERR_INVALID, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
   // one staging copy: per problem [ray records][parallel directions][elements],
-  // then the problems' launch descriptors and the two block-offset tables
-  struct Part { size_t oV, oD, oE, oRec; };
+  // then the problems' launch descriptors and the block-offset table
+  struct Part { size_t oV, oD, oE; };
   std::vector<Part> parts(n);
   size_t total = 0;
   for (int k = 0; k < n; k++) {
@@ -890,8 +884,6 @@ int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
   }
   const size_t oP = total;
   total = up16(total + sizeof(RaysumLaunch) * n);
-  const size_t oS = total;
-  total = up16(total + sizeof(int) * (n + 1));
   const size_t oR = total;
   total = up16(total + sizeof(int) * (n + 1));
   ctgpu_scanner* s0 = scanners[0];
@@ -901,8 +893,8 @@ int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
   int slot = 0;
   CUDA_TRY(stage_host(s0, total, &h, &slot));
   std::vector<RaysumLaunch> L(n);
-  std::vector<int> setupStart(n + 1, 0), rayStart(n + 1, 0);
-  size_t smem = 0, recBytes = 0;
+  std::vector<int> rayStart(n + 1, 0);
+  size_t smem = 0;
   for (int k = 0; k < n; k++) {
     ctgpu_scanner* s = scanners[k];
     const ctgpu_phantom* p = phantoms[k];
@@ -932,21 +924,14 @@ int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
     q.nSlices = 1;
     const size_t sm = raysum_prepare(q);
     if (sm > smem) smem = sm;
-    parts[k].oRec = recBytes;
-    recBytes = (recBytes + raysum_record_bytes(q, q.nElem) + 255) & ~(size_t)255;
-    setupStart[k + 1] = setupStart[k] + raysum_setup_blocks(q);
     rayStart[k + 1] = rayStart[k] + nv;
   }
-  CUDA_TRY(ensure_device(s0->d_records, s0->d_records_cap, recBytes));
-  for (int k = 0; k < n; k++) L[k].records = s0->d_records + parts[k].oRec;
   std::memcpy(h + oP, L.data(), sizeof(RaysumLaunch) * n);
-  std::memcpy(h + oS, setupStart.data(), sizeof(int) * (n + 1));
   std::memcpy(h + oR, rayStart.data(), sizeof(int) * (n + 1));
   CUDA_TRY(stage_send(s0, slot, total, st));
   cudaError_t e = launch_raysum_multi(reinterpret_cast<const RaysumLaunch*>(s0->d_stage + oP),
-                                      reinterpret_cast<const int*>(s0->d_stage + oS),
-                                      setupStart[n], reinterpret_cast<const int*>(s0->d_stage + oR),
-                                      rayStart[n], n, smem, st);
+                                      reinterpret_cast<const int*>(s0->d_stage + oR), rayStart[n],
+                                      n, smem, st);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "too many phantom elements x rays per detector for one CTA");
   CUDA_TRY(e);
@@ -1004,9 +989,6 @@ int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ell, in
   L.sino = d_sino;
   L.status = status_pointer();
   L.elemsPerView = 1;
-  // records: one per (view, ellipsoid, ray sample), as for nView x n elements
-  CUDA_TRY(ensure_device(s->d_records, s->d_records_cap, raysum_record_bytes(L, n)));
-  L.records = s->d_records;
   cudaError_t e = launch_raysum(L, st);
   if (e == cudaErrorInvalidValue)
     return fail(CTGPU_ERR_UNSUPPORTED, "too many ellipsoids x rays per detector for one CTA");

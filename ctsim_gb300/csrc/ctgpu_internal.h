@@ -74,7 +74,6 @@ struct RaysumLaunch {
   const float2* sdirs;    // parallel: [nViews][nSample] unit ray directions
   const double2* arc;     // equiangular: (cos, sin) of t * delta, t < nDet * nSample
   const float2* arcHalf;  // equiangular: (cos, sin) of t * delta / 2 (FP32)
-  void* records;          // scratch: raysum_record_bytes()
   float* sino;
   unsigned int* status;
   // several phantoms, one sinogram each (grid.y): phantom z's elements are
@@ -87,7 +86,7 @@ struct RaysumLaunch {
   // at elems + v * nElem; an element of type < 0 is absent from that view
   int elemsPerView;
   // set by launch_raysum: 1 / centerDetectorLength, and atan(j / 64) for
-  // j = 0..64 (the record set-up's table-driven arctangent)
+  // j = 0..64 (the element records' table-driven arctangent)
   double invCD;
   double atan64[65];
 };
@@ -242,18 +241,13 @@ cudaError_t launch_ellipsoid_sections(const PElem* base, const double2* zc, int 
 // element (ellipses) into grad[6 * nElem] (FP64, accumulated: zero it first)
 cudaError_t launch_raysum_ellipse_grad(const RaysumLaunch& L, const float* gsino, double* grad,
                                        cudaStream_t s);
-// scratch of launch_raysum: one record per (phantom, view, element, ray sample)
-size_t raysum_record_bytes(const RaysumLaunch& L, int totalElems);
 // Many scans (each its own geometry, detectors, views and phantom) in one
-// set-up and one ray launch.  raysum_prepare completes a descriptor (1/CD,
-// the arctangent table) and returns its ray blocks' shared memory;
-// raysum_setup_blocks gives its set-up blocks.  d_probs: the n descriptors in
-// device memory; d_setupStart / d_rayStart: n + 1 block offsets each.
+// ray launch.  raysum_prepare completes a descriptor (1/CD, the arctangent
+// table) and returns its ray blocks' shared memory.  d_probs: the n
+// descriptors in device memory; d_rayStart: n + 1 block offsets.
 size_t raysum_prepare(RaysumLaunch& L);
-int raysum_setup_blocks(const RaysumLaunch& L);
-cudaError_t launch_raysum_multi(const RaysumLaunch* d_probs, const int* d_setupStart,
-                                int setupBlocks, const int* d_rayStart, int rayBlocks, int n,
-                                size_t smem, cudaStream_t s);
+cudaError_t launch_raysum_multi(const RaysumLaunch* d_probs, const int* d_rayStart,
+                                int rayBlocks, int n, size_t smem, cudaStream_t s);
 cudaError_t launch_unit_pulse(float* sino, int nViews, int nDet, int pitch, int rowOffset,
                               cudaStream_t s);
 // *rowsWritten (if given): whether the launch also wrote L.rows

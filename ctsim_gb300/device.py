@@ -77,7 +77,7 @@ def raysums_batch(scanner, phantoms, sinos, stream=None):
 
 def raysums_multi(scanners, phantoms, sinos, stream=None):
     """collectProjections of many (scanner, phantom) problems of different
-    geometry, detectors and views in one set-up and one ray launch
+    geometry, detectors and views in one ray launch
     (ctgpu_collect_projections_multi): sinos[k] a device [n_view_k, pitch_k]
     tensor; returns the view angles of every problem."""
     n = len(scanners)

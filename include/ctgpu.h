@@ -135,7 +135,7 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
                                     int n_phantoms, float* d_sinos, int sino_pitch,
                                     long long sino_slice_stride, double* h_view_angles,
                                     void* stream);
-/* Many scans of uneven shapes in one set-up launch and one ray launch: problem
+/* Many scans of uneven shapes in one ray launch: problem
  * k scans phantoms[k] with scanners[k] (each its own geometry, nDet, nView
  * and nSample) over all its views into d_sinos[k] (rows of sino_pitches[k]
  * floats) and, if h_view_angles and h_view_angles[k] are not NULL, stores its

@@ -1,4 +1,4 @@
-"""Many scans of uneven shapes in one set-up launch and one ray launch
+"""Many scans of uneven shapes in one ray launch
 (ctgpu_collect_projections_multi): every geometry, 1-3 rays per detector,
 detector counts from 101 to 1434, view counts from 60 to 1440, built-in,
 file and random phantoms (all element types).  Each problem's sinogram and
