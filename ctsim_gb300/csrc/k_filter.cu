@@ -380,17 +380,20 @@ template <int LOG2N>
 static cudaError_t launch_persistent(const FilterLaunch& L, cudaStream_t s, bool* rowsWritten) {
   constexpr int T = (1 << LOG2N) / 16;
   auto kern = fft_filter_persistent_kernel<LOG2N>;
-  static int perSm = 0, sms = 0;
-  if (!perSm) {
-    int dev = 0;
+  // resident blocks of this kernel on the device, queried once (thread-safe
+  // initialisation; 0 if the query failed)
+  static const long long resident = [] {
+    int dev = 0, sms = 0, perSm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, T, 0) != cudaSuccess ||
-        perSm < 1)
-      return cudaErrorInvalidValue;
-  }
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fft_filter_persistent_kernel<LOG2N>,
+                                                      (1 << LOG2N) / 16, 0) != cudaSuccess)
+      return 0LL;
+    return (long long)sms * perSm;
+  }();
+  if (resident < 1) return cudaErrorInvalidValue;
   const long long units = (long long)((L.nViews + 1) / 2) * (L.nBatch > 0 ? L.nBatch : 1);
-  const long long grid = std::min<long long>(units, (long long)sms * perSm);
+  const long long grid = std::min<long long>(units, resident);
   const int vec = ((reinterpret_cast<uintptr_t>(L.in) | reinterpret_cast<uintptr_t>(L.out) |
                     reinterpret_cast<uintptr_t>(L.weights)) & 15) == 0 &&
                   (L.inPitch & 3) == 0 && (L.outPitch & 3) == 0 && (L.inSliceStride & 3) == 0 &&
