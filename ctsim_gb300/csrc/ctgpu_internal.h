@@ -85,8 +85,9 @@ struct RaysumLaunch {
   // one element list per view (3-D phantoms): view v's nElem elements start
   // at elems + v * nElem; an element of type < 0 is absent from that view
   int elemsPerView;
-  // set by launch_raysum: 1 / centerDetectorLength, and atan(j / 64) for
-  // j = 0..64 (the element records' table-driven arctangent)
+  // set by launch_raysum: views per ray block, 1 / centerDetectorLength, and
+  // atan(j / 64) for j = 0..64 (the element records' table-driven arctangent)
+  int viewsPerBlock;
   double invCD;
   double atan64[65];
 };

@@ -406,161 +406,178 @@ __device__ void setup_element(const RaysumLaunch& L, const RayView& g, const flo
 
 }  // namespace
 
-// One view of one phantom's sinogram (ev: the block's shared memory).
+// Views view0 .. view0 + nvb - 1 of one phantom's sinogram (ev0: the block's
+// shared memory, the views' records one after another, then their parallel
+// ray directions).
 template <int GEOM>
-__device__ __forceinline__ void ray_block(const RaysumLaunch& L, int view, int z, ElemView* ev) {
+__device__ __forceinline__ void ray_block(const RaysumLaunch& L, int view0, int nvb, int z,
+                                          ElemView* ev0) {
   const int nS = L.nSample;
   const int nSub = (GEOM == kParallel) ? nS : 1;
-  const PElem* elems = L.elems;
+  const PElem* elems0 = L.elems;
   int off = 0, nElem = L.nElem;
   float* sino = L.sino + (size_t)z * L.sliceStride;
   if (L.elemOffset) {
     off = L.elemOffset[z];
     nElem = L.elemOffset[z + 1] - off;
-    elems += off;
+    elems0 += off;
   }
-  if (L.elemsPerView) elems += (size_t)view * nElem;
-  const RayView& g = L.views[view];
-  // this view's (element, ray sample) records, built in FP64 by the block's
+  const int recStride = L.nElem * nSub;   // shared-memory records per view
+  // the views' (element, ray sample) records, built in FP64 by the block's
   // first threads straight into shared memory.  FP64 runs at 1/64 of the FP32
   // rate here and these warps are partly idle, but their set-up overlaps the
-  // rays of the SM's other blocks: measured on 64 phantoms x 720 views against
-  // a separate full-warp set-up launch, equiangular 0.516 -> 0.510 ms,
-  // equilinear 0.442 -> 0.375 ms, parallel with 3 rays per detector
-  // 1.177 -> 0.943 ms (same sums, bit for bit)
+  // rays of the SM's other blocks, and one set-up pass serves the rays of
+  // several views.  Measured on 64 phantoms x 720 views against a separate
+  // full-warp set-up launch: equiangular 0.516 -> 0.510 ms with one view per
+  // block, 0.452 ms with 4; equilinear 0.442 -> 0.379 / 0.355 ms; parallel
+  // with 3 rays per detector 1.177 -> 0.943 ms, 0.921 ms with 2 views (same
+  // sums, bit for bit)
   {
     const int per = nElem * nSub;
-    for (int k = threadIdx.x; k < per; k += blockDim.x)
-      setup_element<GEOM>(L, g, L.sdirs, elems[k / nSub], k % nSub, ev[k]);
+    for (int k = threadIdx.x; k < per * nvb; k += blockDim.x) {
+      const int j = k / per, kk = k - j * per;
+      const PElem* el = elems0 + (L.elemsPerView ? (size_t)(view0 + j) * nElem : 0);
+      setup_element<GEOM>(L, L.views[view0 + j], L.sdirs, el[kk / nSub], kk % nSub,
+                          ev0[j * recStride + kk]);
+    }
   }
-  float2* sdir = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(ev) +
-                                           dir_table_offset(L.nElem * nSub));   // per sub-sample
+  float2* sdir0 = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(ev0) +
+                                            dir_table_offset(nvb * recStride));
   if (GEOM == kParallel)
-    for (int i = threadIdx.x; i < nS; i += blockDim.x) sdir[i] = L.sdirs[(size_t)view * nS + i];
+    for (int i = threadIdx.x; i < nS * nvb; i += blockDim.x)
+      sdir0[i] = L.sdirs[(size_t)view0 * nS + i];
   __syncthreads();
 
-  const float rsx = g.rsx, rsy = g.rsy, stx = g.stx, sty = g.sty;
-  const float hdelta = g.hdelta, fca0 = g.ca0, fsa0 = g.sa0, Sx = g.Sx, Sy = g.Sy;
-  const float CD = (float)L.centerDetectorLength;
+  for (int j = 0; j < nvb; j++) {
+    const int view = view0 + j;
+    const PElem* elems = elems0 + (L.elemsPerView ? (size_t)view * nElem : 0);
+    const ElemView* ev = ev0 + j * recStride;
+    const float2* sdir = sdir0 + j * nS;   // per sub-sample
+    const RayView& g = L.views[view];
+    const float rsx = g.rsx, rsy = g.rsy, stx = g.stx, sty = g.sty;
+    const float hdelta = g.hdelta, fca0 = g.ca0, fsa0 = g.sa0, Sx = g.Sx, Sy = g.Sy;
+    const float CD = (float)L.centerDetectorLength;
 
-  // ray indices as floats by float arithmetic (exact below 2^24), not by
-  // int-to-float conversions
-  const float fnS = (float)nS, fstep = (float)blockDim.x;
-  float fd = (float)threadIdx.x;
-  for (int d = threadIdx.x; d < L.nDet; d += blockDim.x, fd += fstep) {
-    float sum = 0.f;
-    float fi = 0.f;
-    for (int i = 0; i < nS; i++, fi += 1.f) {
-      const int t = (GEOM == kParallel) ? d : d * nS + i;
-      const float ft = (GEOM == kParallel) ? fd : fmaf(fd, fnS, fi);
-      float rx, ry, invr = 1.f, cj = 1.f, sj = 0.f;
-      if (GEOM == kParallel) {
-        rx = sdir[i].x;
-        ry = sdir[i].y;
-      } else if (GEOM == kEquilinear) {
-        rx = fmaf(ft, stx, rsx);
-        ry = fmaf(ft, sty, rsy);
-        invr = rsqrtf(fmaf(rx, rx, ry * ry));
-        rx *= invr;
-        ry *= invr;
-      } else {
-        // cos, sin of phi_t / 2 (phi_t = t * delta) from the scanner's table
-        const float2 cs = __ldg(&L.arcHalf[t]);
-        cj = cs.x;
-        sj = cs.y;
-        float cphi = fmaf(-2.f * sj, sj, 1.f), sphi = 2.f * sj * cj;
-        float dxv = CD * (fca0 * cphi - fsa0 * sphi), dyv = CD * (fsa0 * cphi + fca0 * sphi);
-        rx = dxv - Sx;
-        ry = dyv - Sy;
-        invr = rsqrtf(fmaf(rx, rx, ry * ry));
-        rx *= invr;
-        ry *= invr;
-      }
-      // the elements whose ray range meets this warp's rays: lane j tests
-      // element kb + j, a ballot collects them, and the loop visits them in
-      // ascending order (the sums keep their order).  The warp's lanes in this
-      // iteration are the detectors dw0 .. dwm, all of them here.
-      const int dw0 = d - (int)(threadIdx.x & 31), dwm = min(dw0 + 31, L.nDet - 1);
-      const unsigned wmask = dwm - dw0 >= 31 ? 0xffffffffu : (1u << (dwm - dw0 + 1)) - 1u;
-      const int twlo = (GEOM == kParallel) ? dw0 : dw0 * nS + i;
-      const int twhi = (GEOM == kParallel) ? dwm : dwm * nS + i;
-      for (int kb = 0; kb < nElem; kb += 32) {
-        const int kl = kb + (int)(threadIdx.x & 31);
-        bool meets = false;
-        if (kl < nElem) {
-          const int2 r = *reinterpret_cast<const int2*>(&ev[kl * nSub + (GEOM == kParallel ? i : 0)]);
-          meets = !(twhi < r.x || twlo > r.y);
+    // ray indices as floats by float arithmetic (exact below 2^24), not by
+    // int-to-float conversions
+    const float fnS = (float)nS, fstep = (float)blockDim.x;
+    float fd = (float)threadIdx.x;
+    for (int d = threadIdx.x; d < L.nDet; d += blockDim.x, fd += fstep) {
+      float sum = 0.f;
+      float fi = 0.f;
+      for (int i = 0; i < nS; i++, fi += 1.f) {
+        const int t = (GEOM == kParallel) ? d : d * nS + i;
+        const float ft = (GEOM == kParallel) ? fd : fmaf(fd, fnS, fi);
+        float rx, ry, invr = 1.f, cj = 1.f, sj = 0.f;
+        if (GEOM == kParallel) {
+          rx = sdir[i].x;
+          ry = sdir[i].y;
+        } else if (GEOM == kEquilinear) {
+          rx = fmaf(ft, stx, rsx);
+          ry = fmaf(ft, sty, rsy);
+          invr = rsqrtf(fmaf(rx, rx, ry * ry));
+          rx *= invr;
+          ry *= invr;
+        } else {
+          // cos, sin of phi_t / 2 (phi_t = t * delta) from the scanner's table
+          const float2 cs = __ldg(&L.arcHalf[t]);
+          cj = cs.x;
+          sj = cs.y;
+          float cphi = fmaf(-2.f * sj, sj, 1.f), sphi = 2.f * sj * cj;
+          float dxv = CD * (fca0 * cphi - fsa0 * sphi), dyv = CD * (fsa0 * cphi + fca0 * sphi);
+          rx = dxv - Sx;
+          ry = dyv - Sy;
+          invr = rsqrtf(fmaf(rx, rx, ry * ry));
+          rx *= invr;
+          ry *= invr;
         }
-        unsigned todo = __ballot_sync(wmask, meets);
-        while (todo) {
-          const int k = kb + __ffs(todo) - 1;
-          todo &= todo - 1;
-          const ElemView& e = ev[k * nSub + (GEOM == kParallel ? i : 0)];
-          const int4 hdr = *reinterpret_cast<const int4*>(&e);
-          if (t < hdr.x || t > hdr.y) continue;
-          // integers below 2^24: (float)tcI - ft is the exact (float)(tcI - t)
-          const float ftc = __int_as_float(hdr.z), tcF = __int_as_float(hdr.w);
-          const float4 w1 = ld4(&e.kB);     // kB, cpsi, spsi, rbox
-          float rho;
-          if (GEOM == kEquiangular) {
-            float x = ((ftc - ft) + tcF) * hdelta;
-            float cf = fmaf(w1.y, cj, w1.z * sj);
-            rho = w1.x * cf * sin_series(x) * invr;
-          } else {
-            float dt = (ft - ftc) - tcF;
-            rho = w1.x * dt * invr;
+        // the elements whose ray range meets this warp's rays: lane j tests
+        // element kb + j, a ballot collects them, and the loop visits them in
+        // ascending order (the sums keep their order).  The warp's lanes in this
+        // iteration are the detectors dw0 .. dwm, all of them here.
+        const int dw0 = d - (int)(threadIdx.x & 31), dwm = min(dw0 + 31, L.nDet - 1);
+        const unsigned wmask = dwm - dw0 >= 31 ? 0xffffffffu : (1u << (dwm - dw0 + 1)) - 1u;
+        const int twlo = (GEOM == kParallel) ? dw0 : dw0 * nS + i;
+        const int twhi = (GEOM == kParallel) ? dwm : dwm * nS + i;
+        for (int kb = 0; kb < nElem; kb += 32) {
+          const int kl = kb + (int)(threadIdx.x & 31);
+          bool meets = false;
+          if (kl < nElem) {
+            const int2 r = *reinterpret_cast<const int2*>(&ev[kl * nSub + (GEOM == kParallel ? i : 0)]);
+            meets = !(twhi < r.x || twlo > r.y);
           }
-          // cull against the outline box's circumcircle
-          const float4 w2 = ld4(&e.dcbx);   // dcbx, dcby, rin, type
-          float rhob = rho + (rx * w2.y - ry * w2.x);
-          const float arhob = fabsf(rhob);
-          if (arhob > w1.w) continue;
-          float ch;
-          if (__float_as_int(w2.w) == kEllipse) {
-            ch = ellipse_chord(ld4(&e.qa), rho, rx, ry);
-          } else {
-            float ra, rb;
-            if (GEOM == kParallel) { ra = e.ra; rb = e.rb; }
-            else { ra = rx * e.ca + ry * e.sa; rb = -rx * e.sa + ry * e.ca; }
-            ch = element_chord(e, rho, rx, ry, ra, rb);
-          }
-          if (ch <= 0.f) continue;
-          const float4 w4 = ld4(&e.hx);     // hx, hy, atten, tcI
-          int bt = arhob < w2.z ? 1 : box_test(w4.x, w4.y, rhob, rx, ry);
-          if (bt == 0) {
-            // within the FP32 test's margin: decide in FP64 on this ray's end
-            // points whether its line meets the outline box
-            const PElem& pe = elems[k];
-            double xd, yd, xs, ys;
+          unsigned todo = __ballot_sync(wmask, meets);
+          while (todo) {
+            const int k = kb + __ffs(todo) - 1;
+            todo &= todo - 1;
+            const ElemView& e = ev[k * nSub + (GEOM == kParallel ? i : 0)];
+            const int4 hdr = *reinterpret_cast<const int4*>(&e);
+            if (t < hdr.x || t > hdr.y) continue;
+            // integers below 2^24: (float)tcI - ft is the exact (float)(tcI - t)
+            const float ftc = __int_as_float(hdr.z), tcF = __int_as_float(hdr.w);
+            const float4 w1 = ld4(&e.kB);     // kB, cpsi, spsi, rbox
+            float rho;
             if (GEOM == kEquiangular) {
-              // detector point at arc angle alpha0 + t delta, by the angle sum
-              const double2 a = L.arc[t];
-              xd = L.centerDetectorLength * (g.c0 * a.x - g.s0 * a.y);
-              yd = L.centerDetectorLength * (g.s0 * a.x + g.c0 * a.y);
-              xs = g.S0x;
-              ys = g.S0y;
+              float x = ((ftc - ft) + tcF) * hdelta;
+              float cf = fmaf(w1.y, cj, w1.z * sj);
+              rho = w1.x * cf * sin_series(x) * invr;
             } else {
-              xs = g.S0x + (GEOM == kParallel ? d * g.dSx : 0.0);
-              ys = g.S0y + (GEOM == kParallel ? d * g.dSy : 0.0);
-              int tt = d * nS + i;
-              xd = g.D0x + (double)tt * g.dDx;
-              yd = g.D0y + (double)tt * g.dDy;
+              float dt = (ft - ftc) - tcF;
+              rho = w1.x * dt * invr;
             }
-            bt = line_meets_box_fp64(xs, ys, xd, yd, pe) ? 1 : -1;
+            // cull against the outline box's circumcircle
+            const float4 w2 = ld4(&e.dcbx);   // dcbx, dcby, rin, type
+            float rhob = rho + (rx * w2.y - ry * w2.x);
+            const float arhob = fabsf(rhob);
+            if (arhob > w1.w) continue;
+            float ch;
+            if (__float_as_int(w2.w) == kEllipse) {
+              ch = ellipse_chord(ld4(&e.qa), rho, rx, ry);
+            } else {
+              float ra, rb;
+              if (GEOM == kParallel) { ra = e.ra; rb = e.rb; }
+              else { ra = rx * e.ca + ry * e.sa; rb = -rx * e.sa + ry * e.ca; }
+              ch = element_chord(e, rho, rx, ry, ra, rb);
+            }
+            if (ch <= 0.f) continue;
+            const float4 w4 = ld4(&e.hx);     // hx, hy, atten, tcI
+            int bt = arhob < w2.z ? 1 : box_test(w4.x, w4.y, rhob, rx, ry);
+            if (bt == 0) {
+              // within the FP32 test's margin: decide in FP64 on this ray's end
+              // points whether its line meets the outline box
+              const PElem& pe = elems[k];
+              double xd, yd, xs, ys;
+              if (GEOM == kEquiangular) {
+                // detector point at arc angle alpha0 + t delta, by the angle sum
+                const double2 a = L.arc[t];
+                xd = L.centerDetectorLength * (g.c0 * a.x - g.s0 * a.y);
+                yd = L.centerDetectorLength * (g.s0 * a.x + g.c0 * a.y);
+                xs = g.S0x;
+                ys = g.S0y;
+              } else {
+                xs = g.S0x + (GEOM == kParallel ? d * g.dSx : 0.0);
+                ys = g.S0y + (GEOM == kParallel ? d * g.dSy : 0.0);
+                int tt = d * nS + i;
+                xd = g.D0x + (double)tt * g.dDx;
+                yd = g.D0y + (double)tt * g.dDy;
+              }
+              bt = line_meets_box_fp64(xs, ys, xd, yd, pe) ? 1 : -1;
+            }
+            if (bt < 0) continue;
+            sum = fmaf(ch, w4.z, sum);
           }
-          if (bt < 0) continue;
-          sum = fmaf(ch, w4.z, sum);
         }
       }
+      sino[(size_t)(L.rowOffset + view) * L.pitch + d] = sum / fnS;
     }
-    sino[(size_t)(L.rowOffset + view) * L.pitch + d] = sum / fnS;
   }
 }
 
 template <int GEOM>
 __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
   extern __shared__ __align__(16) ElemView ev[];
-  ray_block<GEOM>(L, blockIdx.x, blockIdx.y, ev);
+  const int v0 = blockIdx.x * L.viewsPerBlock;
+  ray_block<GEOM>(L, v0, min(L.viewsPerBlock, L.nViews - v0), blockIdx.y, ev);
 }
 
 // Many scans in one launch each: problem k's descriptor is probs[k] (in
@@ -585,9 +602,9 @@ __global__ void __launch_bounds__(128, 4) raysum_multi_kernel(const RaysumLaunch
   const RaysumLaunch& L = probs[k];
   const int view = blockIdx.x - blockStart[k];
   switch (L.geometry) {
-    case kParallel: ray_block<kParallel>(L, view, 0, ev); break;
-    case kEquilinear: ray_block<kEquilinear>(L, view, 0, ev); break;
-    default: ray_block<kEquiangular>(L, view, 0, ev); break;
+    case kParallel: ray_block<kParallel>(L, view, 1, 0, ev); break;
+    case kEquilinear: ray_block<kEquilinear>(L, view, 1, 0, ev); break;
+    default: ray_block<kEquiangular>(L, view, 1, 0, ev); break;
   }
 }
 
@@ -605,9 +622,16 @@ static cudaError_t raysum_launch(const RaysumLaunch& L, size_t smem, int nSlices
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  dim3 grid(L.nViews, nSlices);
+  dim3 grid((L.nViews + L.viewsPerBlock - 1) / L.viewsPerBlock, nSlices);
   raysum_kernel<GEOM><<<grid, 128, smem, s>>>(L);
   return cudaGetLastError();
+}
+
+// shared memory of a ray block of vpb views (records, then parallel directions)
+static size_t raysum_smem(const RaysumLaunch& L, int vpb) {
+  const int nSub = (L.geometry == kParallel) ? L.nSample : 1;
+  return dir_table_offset((size_t)vpb * (L.nElem > 0 ? L.nElem : 1) * nSub) +
+         sizeof(float2) * (size_t)L.nSample * vpb;
 }
 
 cudaError_t launch_raysum(const RaysumLaunch& L0, cudaStream_t s) {
@@ -615,9 +639,14 @@ cudaError_t launch_raysum(const RaysumLaunch& L0, cudaStream_t s) {
   RaysumLaunch L = L0;
   L.invCD = L.centerDetectorLength != 0.0 ? 1.0 / L.centerDetectorLength : 0.0;
   std::copy(atan64_table().v, atan64_table().v + 65, L.atan64);
-  int nSub = (L.geometry == kParallel) ? L.nSample : 1;
-  size_t smem = dir_table_offset((L.nElem > 0 ? L.nElem : 1) * nSub) +
-                sizeof(float2) * (size_t)L.nSample;
+  // views per block: 4, or 2 for several rays per detector (measured best
+  // of 1, 2, 4, 6, 8 on 64 phantoms x 720 views), fewer where their records
+  // would not fit the 48 KB a block gets without opting in
+  const int nSub = (L.geometry == kParallel) ? L.nSample : 1;
+  int vpb = nSub > 1 ? 2 : 4;
+  while (vpb > 1 && raysum_smem(L, vpb) > 48 * 1024) vpb--;
+  L.viewsPerBlock = vpb;
+  const size_t smem = raysum_smem(L, vpb);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   const int nSlices = L.nSlices > 0 ? L.nSlices : 1;
   if (nSlices > 65535) return cudaErrorInvalidConfiguration;
@@ -631,9 +660,8 @@ cudaError_t launch_raysum(const RaysumLaunch& L0, cudaStream_t s) {
 size_t raysum_prepare(RaysumLaunch& L) {
   L.invCD = L.centerDetectorLength != 0.0 ? 1.0 / L.centerDetectorLength : 0.0;
   std::copy(atan64_table().v, atan64_table().v + 65, L.atan64);
-  const int nSub = (L.geometry == kParallel) ? L.nSample : 1;
-  return dir_table_offset((L.nElem > 0 ? L.nElem : 1) * nSub) +
-         sizeof(float2) * (size_t)L.nSample;
+  L.viewsPerBlock = 1;
+  return raysum_smem(L, 1);
 }
 
 cudaError_t launch_raysum_multi(const RaysumLaunch* d_probs, const int* d_rayStart,
