@@ -924,7 +924,7 @@ int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
     q.nSlices = 1;
     const size_t sm = raysum_prepare(q);
     if (sm > smem) smem = sm;
-    rayStart[k + 1] = rayStart[k] + nv;
+    rayStart[k + 1] = rayStart[k] + (nv + q.viewsPerBlock - 1) / q.viewsPerBlock;
   }
   std::memcpy(h + oP, L.data(), sizeof(RaysumLaunch) * n);
   std::memcpy(h + oR, rayStart.data(), sizeof(int) * (n + 1));

@@ -243,9 +243,10 @@ cudaError_t launch_ellipsoid_sections(const PElem* base, const double2* zc, int 
 cudaError_t launch_raysum_ellipse_grad(const RaysumLaunch& L, const float* gsino, double* grad,
                                        cudaStream_t s);
 // Many scans (each its own geometry, detectors, views and phantom) in one
-// ray launch.  raysum_prepare completes a descriptor (1/CD, the arctangent
-// table) and returns its ray blocks' shared memory.  d_probs: the n
-// descriptors in device memory; d_rayStart: n + 1 block offsets.
+// ray launch.  raysum_prepare completes a descriptor (views per block, 1/CD,
+// the arctangent table) and returns its ray blocks' shared memory.  d_probs:
+// the n descriptors in device memory; d_rayStart: n + 1 block offsets (a
+// problem has ceil(nViews / viewsPerBlock) blocks).
 size_t raysum_prepare(RaysumLaunch& L);
 cudaError_t launch_raysum_multi(const RaysumLaunch* d_probs, const int* d_rayStart,
                                 int rayBlocks, int n, size_t smem, cudaStream_t s);

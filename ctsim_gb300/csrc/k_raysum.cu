@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(128) raysum_kernel(RaysumLaunch L) {
 
 // Many scans in one launch each: problem k's descriptor is probs[k] (in
 // device memory), and its blocks are blockStart[k] .. blockStart[k+1) of the
-// grid, one per view.
+// grid, one per viewsPerBlock views.
 __device__ __forceinline__ int problem_of_block(const int* __restrict__ blockStart, int n) {
   int lo = 0, hi = n - 1;
   const int b = blockIdx.x;
@@ -600,11 +600,12 @@ __global__ void __launch_bounds__(128, 4) raysum_multi_kernel(const RaysumLaunch
   extern __shared__ __align__(16) ElemView ev[];
   const int k = problem_of_block(blockStart, n);
   const RaysumLaunch& L = probs[k];
-  const int view = blockIdx.x - blockStart[k];
+  const int v0 = (blockIdx.x - blockStart[k]) * L.viewsPerBlock;
+  const int nvb = min(L.viewsPerBlock, L.nViews - v0);
   switch (L.geometry) {
-    case kParallel: ray_block<kParallel>(L, view, 1, 0, ev); break;
-    case kEquilinear: ray_block<kEquilinear>(L, view, 1, 0, ev); break;
-    default: ray_block<kEquiangular>(L, view, 1, 0, ev); break;
+    case kParallel: ray_block<kParallel>(L, v0, nvb, 0, ev); break;
+    case kEquilinear: ray_block<kEquilinear>(L, v0, nvb, 0, ev); break;
+    default: ray_block<kEquiangular>(L, v0, nvb, 0, ev); break;
   }
 }
 
@@ -634,19 +635,23 @@ static size_t raysum_smem(const RaysumLaunch& L, int vpb) {
          sizeof(float2) * (size_t)L.nSample * vpb;
 }
 
+// views per ray block: 4, or 2 for several rays per detector (measured best
+// of 1, 2, 4, 6, 8 on 64 phantoms x 720 views), fewer where their records
+// would not fit the 48 KB a block gets without opting in
+static int raysum_views_per_block(const RaysumLaunch& L) {
+  const int nSub = (L.geometry == kParallel) ? L.nSample : 1;
+  int vpb = nSub > 1 ? 2 : 4;
+  while (vpb > 1 && raysum_smem(L, vpb) > 48 * 1024) vpb--;
+  return vpb;
+}
+
 cudaError_t launch_raysum(const RaysumLaunch& L0, cudaStream_t s) {
   if (L0.nViews <= 0) return cudaSuccess;
   RaysumLaunch L = L0;
   L.invCD = L.centerDetectorLength != 0.0 ? 1.0 / L.centerDetectorLength : 0.0;
   std::copy(atan64_table().v, atan64_table().v + 65, L.atan64);
-  // views per block: 4, or 2 for several rays per detector (measured best
-  // of 1, 2, 4, 6, 8 on 64 phantoms x 720 views), fewer where their records
-  // would not fit the 48 KB a block gets without opting in
-  const int nSub = (L.geometry == kParallel) ? L.nSample : 1;
-  int vpb = nSub > 1 ? 2 : 4;
-  while (vpb > 1 && raysum_smem(L, vpb) > 48 * 1024) vpb--;
-  L.viewsPerBlock = vpb;
-  const size_t smem = raysum_smem(L, vpb);
+  L.viewsPerBlock = raysum_views_per_block(L);
+  const size_t smem = raysum_smem(L, L.viewsPerBlock);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   const int nSlices = L.nSlices > 0 ? L.nSlices : 1;
   if (nSlices > 65535) return cudaErrorInvalidConfiguration;
@@ -660,8 +665,8 @@ cudaError_t launch_raysum(const RaysumLaunch& L0, cudaStream_t s) {
 size_t raysum_prepare(RaysumLaunch& L) {
   L.invCD = L.centerDetectorLength != 0.0 ? 1.0 / L.centerDetectorLength : 0.0;
   std::copy(atan64_table().v, atan64_table().v + 65, L.atan64);
-  L.viewsPerBlock = 1;
-  return raysum_smem(L, 1);
+  L.viewsPerBlock = raysum_views_per_block(L);
+  return raysum_smem(L, L.viewsPerBlock);
 }
 
 cudaError_t launch_raysum_multi(const RaysumLaunch* d_probs, const int* d_rayStart,
