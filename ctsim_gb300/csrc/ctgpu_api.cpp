@@ -236,9 +236,14 @@ struct ctgpu_scanner {
   double fanBeamAngle, xCenter, yCenter, angularDetLen = 0, angularDetInc = 0;
   double xs1, ys1, xs2, ys2, xd1 = 0, yd1 = 0, xd2 = 0, yd2 = 0;
   M3 inc;
+  // the views of the last range asked for (viewsFirst = startView +
+  // offsetView, viewsCount of them), and whether d_views / d_sdirs hold
+  // their ray records: a scanner does not change after create, so both
+  // depend on the range alone and are rebuilt only for another range
   std::vector<ViewPos> views;
-  // collect_projections_ellipsoids, raysum_ellipse_gradient: the views' ray
-  // records and parallel directions
+  int viewsFirst = 0, viewsCount = -1;
+  bool deviceViews = false;
+  // the views' ray records and parallel directions on the device
   RayView* d_views = nullptr;
   size_t d_views_cap = 0;
   float2* d_sdirs = nullptr;
@@ -264,19 +269,18 @@ struct ctgpu_scanner {
   size_t d_half_cap = 0;
   int arcN = 0;
   double arcDelta = 0;
-  // the ray-sum calls' per-call inputs (the views' ray records, parallel ray
-  // directions, elements, offsets) go up as one copy from a page-locked
-  // buffer (two, used in turn: the host fills one while the other's copy may
-  // still be queued) to one device buffer
+  // the batched ray-sum calls' per-call inputs (elements, offsets, launch
+  // descriptors) go up as one copy from a page-locked buffer (two, used in
+  // turn: the host fills one while the other's copy may still be queued) to
+  // one device buffer
   unsigned char* h_stage[2] = {nullptr, nullptr};
   size_t h_stage_cap[2] = {0, 0};
   cudaEvent_t stage_done[2] = {nullptr, nullptr};
   int stage_next = 0;
   unsigned char* d_stage = nullptr;
   size_t d_stage_cap = 0;
-  // ray records and directions are built here, in ordinary host memory, and
-  // moved into the page-locked buffer with one bulk copy (record-by-record
-  // stores into page-locked memory were slower on the Arm hosts)
+  // the ray records and directions of `views`, built on the host for
+  // upload_ray_views
   std::vector<RayView> h_rv;
   std::vector<float2> h_dirs;
   ~ctgpu_scanner() {
@@ -566,6 +570,10 @@ void ctgpu_scanner_destroy(ctgpu_scanner* s) { delete s; }
 
 // View end points by the reference's incremental rotation (scanner.cpp:301-417).
 static void scanner_views(ctgpu_scanner* s, int startView, int nViews, int offsetView) {
+  if (s->viewsCount == nViews && s->viewsFirst == startView + offsetView) return;
+  s->viewsFirst = startView + offsetView;
+  s->viewsCount = nViews;
+  s->deviceViews = false;
   s->views.resize(nViews);
   double start = (startView + offsetView) * s->rotInc;
   M3 m0 = mul(mul(xlat(-s->xCenter, -s->yCenter), rotm(start)), xlat(s->xCenter, s->yCenter));
@@ -676,20 +684,28 @@ static cudaError_t ensure_arc_table(ctgpu_scanner* s) {
   return cudaSuccess;
 }
 
-// the scanner's current views as ray records (+ parallel ray directions) on the device
-static cudaError_t upload_ray_views(ctgpu_scanner* s, int nViews, cudaStream_t st) {
-  std::vector<RayView> rv(nViews);
-  std::vector<float2> dirs(s->geometry == kParallel ? (size_t)nViews * s->nSample : 0);
-  fill_ray_views(s, nViews, rv.data(), dirs.data());
-  cudaError_t e = ensure_device(s->d_views, s->d_views_cap, (size_t)nViews);
+// the scanner's current views (scanner_views) as ray records (+ parallel ray
+// directions) in d_views / d_sdirs, built and uploaded only when the views
+// changed since the last upload.  The copies are from pageable memory: the
+// stream's earlier work (which may read the old records) finishes first.
+static cudaError_t upload_ray_views(ctgpu_scanner* s, cudaStream_t st) {
+  cudaError_t e = ensure_arc_table(s);
+  if (e != cudaSuccess || s->deviceViews) return e;
+  const int nViews = s->viewsCount;
+  s->h_rv.resize(nViews);
+  s->h_dirs.resize(s->geometry == kParallel ? (size_t)nViews * s->nSample : 0);
+  fill_ray_views(s, nViews, s->h_rv.data(), s->h_dirs.data());
+  e = ensure_device(s->d_views, s->d_views_cap, (size_t)(nViews > 0 ? nViews : 1));
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(s->d_views, rv.data(), sizeof(RayView) * nViews, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = ensure_arc_table(s);
-  if (e != cudaSuccess || s->geometry != kParallel) return e;
-  e = ensure_device(s->d_sdirs, s->d_sdirs_cap, dirs.size());
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(s->d_sdirs, dirs.data(), sizeof(float2) * dirs.size(),
+    e = cudaMemcpyAsync(s->d_views, s->h_rv.data(), sizeof(RayView) * nViews,
                         cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && !s->h_dirs.empty()) {
+    e = ensure_device(s->d_sdirs, s->d_sdirs_cap, s->h_dirs.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s->d_sdirs, s->h_dirs.data(), sizeof(float2) * s->h_dirs.size(),
+                          cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess) s->deviceViews = true;
   return e;
 }
 
@@ -723,16 +739,6 @@ static cudaError_t stage_send(ctgpu_scanner* s, int slot, size_t total, cudaStre
   return e;
 }
 static size_t up16(size_t x) { return (x + 15) & ~(size_t)15; }
-// the scanner's current views' ray records (and parallel directions) into a
-// staging buffer at h (directions at h + oD)
-static void stage_ray_views(ctgpu_scanner* s, int nViews, unsigned char* h, size_t oD) {
-  s->h_rv.resize(nViews);
-  s->h_dirs.resize(s->geometry == kParallel ? (size_t)nViews * s->nSample : 0);
-  fill_ray_views(s, nViews, s->h_rv.data(), s->h_dirs.data());
-  std::memcpy(h, s->h_rv.data(), sizeof(RayView) * nViews);
-  if (!s->h_dirs.empty()) std::memcpy(h + oD, s->h_dirs.data(), sizeof(float2) * s->h_dirs.size());
-}
-
 extern "C" {
 
 int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int startView,
@@ -751,16 +757,7 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
     return ok();
   }
   CUDA_TRY(const_cast<ctgpu_phantom*>(p)->upload(st));
-  CUDA_TRY(ensure_arc_table(s));
-  // one staging copy: [ray records][parallel directions]
-  const bool par = s->geometry == kParallel;
-  const size_t oD = up16(sizeof(RayView) * nViews);
-  const size_t total = oD + (par ? sizeof(float2) * nViews * s->nSample : 0);
-  unsigned char* h = nullptr;
-  int slot = 0;
-  CUDA_TRY(stage_host(s, total, &h, &slot));
-  stage_ray_views(s, nViews, h, oD);
-  CUDA_TRY(stage_send(s, slot, total, st));
+  CUDA_TRY(upload_ray_views(s, st));
   RaysumLaunch L{};
   L.geometry = s->geometry;
   L.nDet = s->nDet;
@@ -773,8 +770,8 @@ int ctgpu_collect_projections(ctgpu_scanner* s, const ctgpu_phantom* p, int star
   L.angularDetLen = s->angularDetLen;
   L.angularDetInc = s->angularDetInc;
   L.elems = p->d_elems;
-  L.views = reinterpret_cast<const RayView*>(s->d_stage);
-  L.sdirs = par ? reinterpret_cast<const float2*>(s->d_stage + oD) : nullptr;
+  L.views = s->d_views;
+  L.sdirs = s->geometry == kParallel ? s->d_sdirs : nullptr;
   L.arc = s->d_arc;
   L.arcHalf = s->d_half;
   L.sino = d_sino;
@@ -807,18 +804,14 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   scanner_views(s, 0, s->nView, 0);
   if (h_angles)
     for (int v = 0; v < s->nView; v++) h_angles[v] = s->views[v].angle;
-  CUDA_TRY(ensure_arc_table(s));
-  // one staging copy: [ray records][parallel directions][elements][offsets]
-  const int nv = s->nView;
-  const bool par = s->geometry == kParallel;
-  const size_t oD = up16(sizeof(RayView) * nv);
-  const size_t oE = up16(oD + (par ? sizeof(float2) * nv * s->nSample : 0));
+  CUDA_TRY(upload_ray_views(s, st));
+  // one staging copy: [elements][offsets]
+  const size_t oE = 0;
   const size_t oO = up16(oE + sizeof(PElem) * all.size());
   const size_t total = oO + sizeof(int) * offs.size();
   unsigned char* h = nullptr;
   int slot = 0;
   CUDA_TRY(stage_host(s, total, &h, &slot));
-  stage_ray_views(s, nv, h, oD);
   if (!all.empty()) std::memcpy(h + oE, all.data(), sizeof(PElem) * all.size());
   std::memcpy(h + oO, offs.data(), sizeof(int) * offs.size());
   CUDA_TRY(stage_send(s, slot, total, st));
@@ -834,8 +827,8 @@ int ctgpu_collect_projections_batch(ctgpu_scanner* s, const ctgpu_phantom* const
   L.angularDetLen = s->angularDetLen;
   L.angularDetInc = s->angularDetInc;
   L.elems = reinterpret_cast<const PElem*>(s->d_stage + oE);
-  L.views = reinterpret_cast<const RayView*>(s->d_stage);
-  L.sdirs = par ? reinterpret_cast<const float2*>(s->d_stage + oD) : nullptr;
+  L.views = s->d_views;
+  L.sdirs = s->geometry == kParallel ? s->d_sdirs : nullptr;
   L.arc = s->d_arc;
   L.arcHalf = s->d_half;
   L.sino = d_sinos;
@@ -859,10 +852,10 @@ int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
   if (!scanners || !phantoms || !d_sinos || !pitches || n < 1)
     return fail(CTGPU_ERR_INVALID, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
-  // one staging copy: per problem [ray records][parallel directions][elements],
-  // then the problems' launch descriptors and the block-offset table
-  struct Part { size_t oV, oD, oE; };
-  std::vector<Part> parts(n);
+  // each scanner's ray records and directions stay on the device
+  // (upload_ray_views); one staging copy: per problem its elements, then the
+  // problems' launch descriptors and the block-offset table
+  std::vector<size_t> oE(n);
   size_t total = 0;
   for (int k = 0; k < n; k++) {
     ctgpu_scanner* s = scanners[k];
@@ -874,12 +867,8 @@ int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
     scanner_views(s, 0, s->nView, 0);
     if (h_angles && h_angles[k])
       for (int v = 0; v < s->nView; v++) h_angles[k][v] = s->views[v].angle;
-    CUDA_TRY(ensure_arc_table(s));
-    parts[k].oV = total;
-    total = up16(total + sizeof(RayView) * s->nView);
-    parts[k].oD = total;
-    if (s->geometry == kParallel) total = up16(total + sizeof(float2) * s->nView * s->nSample);
-    parts[k].oE = total;
+    CUDA_TRY(upload_ray_views(s, st));
+    oE[k] = total;
     total = up16(total + sizeof(PElem) * p->elems.size());
   }
   const size_t oP = total;
@@ -899,8 +888,7 @@ int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
     ctgpu_scanner* s = scanners[k];
     const ctgpu_phantom* p = phantoms[k];
     const int nv = s->nView;
-    stage_ray_views(s, nv, h + parts[k].oV, parts[k].oD - parts[k].oV);
-    std::memcpy(h + parts[k].oE, p->elems.data(), sizeof(PElem) * p->elems.size());
+    std::memcpy(h + oE[k], p->elems.data(), sizeof(PElem) * p->elems.size());
     RaysumLaunch& q = L[k];
     q = RaysumLaunch{};
     q.geometry = s->geometry;
@@ -913,10 +901,9 @@ int ctgpu_collect_projections_multi(ctgpu_scanner* const* scanners,
     q.centerDetectorLength = s->centerDetectorLength;
     q.angularDetLen = s->angularDetLen;
     q.angularDetInc = s->angularDetInc;
-    q.elems = reinterpret_cast<const PElem*>(s0->d_stage + parts[k].oE);
-    q.views = reinterpret_cast<const RayView*>(s0->d_stage + parts[k].oV);
-    q.sdirs = s->geometry == kParallel
-                  ? reinterpret_cast<const float2*>(s0->d_stage + parts[k].oD) : nullptr;
+    q.elems = reinterpret_cast<const PElem*>(s0->d_stage + oE[k]);
+    q.views = s->d_views;
+    q.sdirs = s->geometry == kParallel ? s->d_sdirs : nullptr;
     q.arc = s->d_arc;
     q.arcHalf = s->d_half;
     q.sino = d_sinos[k];
@@ -969,7 +956,7 @@ int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ell, in
   CUDA_TRY(launch_ellipsoid_sections(s->d_belems, s->d_zc, n, s->nView, z0, dz, s->d_velems, st));
   // the ray records after the cross-section launch, which runs meanwhile
   // (thousands of views: this call is bound by the host's per-view work)
-  CUDA_TRY(upload_ray_views(s, s->nView, st));
+  CUDA_TRY(upload_ray_views(s, st));
   RaysumLaunch L{};
   L.geometry = s->geometry;
   L.nDet = s->nDet;
@@ -1008,7 +995,7 @@ int ctgpu_raysum_ellipse_gradient(ctgpu_scanner* s, const ctgpu_phantom* p,
   cudaStream_t st = (cudaStream_t)stream;
   scanner_views(s, 0, s->nView, s->offsetView);
   CUDA_TRY(const_cast<ctgpu_phantom*>(p)->upload(st));
-  CUDA_TRY(upload_ray_views(s, s->nView, st));
+  CUDA_TRY(upload_ray_views(s, st));
   double* d_grad = nullptr;
   CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&d_grad), sizeof(double) * 6 * (n > 0 ? n : 1), st));
   RaysumLaunch L{};
