@@ -954,8 +954,8 @@ int ctgpu_collect_projections_ellipsoids(ctgpu_scanner* s, const double* ell, in
   CUDA_TRY(cudaMemcpyAsync(s->d_zc, zc.data(), sizeof(double2) * zc.size(),
                            cudaMemcpyHostToDevice, st));
   CUDA_TRY(launch_ellipsoid_sections(s->d_belems, s->d_zc, n, s->nView, z0, dz, s->d_velems, st));
-  // the ray records after the cross-section launch, which runs meanwhile
-  // (thousands of views: this call is bound by the host's per-view work)
+  // the ray records (built and uploaded on the scanner's first call for
+  // these views) after the cross-section launch, which runs meanwhile
   CUDA_TRY(upload_ray_views(s, st));
   RaysumLaunch L{};
   L.geometry = s->geometry;
