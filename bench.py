@@ -867,9 +867,9 @@ def run_gpu(args):
                                  "peak": fp32_peak, "unit": "TFLOP/s",
                                  "frac": RAYS_PER_SLICE * 12 * B * steps * ray_world * 60 /
                                          (ray_ms / 1e3) / 1e12 / fp32_peak,
-                                 "note": "one launch: each block builds its FP64 element records, "
-                                         "then its rays; ncu: issue slots 74 % busy, FP64 pipe "
-                                         "54 % (profiles/raysum_equiangular_733x720_ncu.md)"},
+                                 "note": "one launch: each block builds the FP64 element records "
+                                         "of its 4 views, then their rays; ncu: issue slots 77 % "
+                                         "busy, FP64 pipe 24 % (profiles/raysum_equiangular_733x720_ncu.md)"},
                     "cpu_baseline": {"value": cpu_raysum_rate[0], "unit": "ray-sums/s",
                                      "cores": cpu_threads, "kind": "port",
                                      "sample": "one 733 x 720 equiangular scan of 12 ellipses"}},
