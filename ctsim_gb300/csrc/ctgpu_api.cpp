@@ -340,23 +340,11 @@ struct ctgpu_recon {
   cudaEvent_t ev[6] = {};   // in_done[2], comp_done[2], out_done[2]
   double* h_angles_pinned = nullptr;   // page-locked copy of the view angles
   size_t h_angles_cap = 0;
-  // ctgpu_recon_run: its own page-locked copy of the angles, so that their
-  // upload does not wait for the stream's earlier work (a pageable copy
-  // would); runAngEv marks the end of the last upload out of it
-  double* h_run_angles = nullptr;
-  size_t h_run_angles_cap = 0;
-  cudaEvent_t runAngEv = nullptr;
-  bool runAngPending = false;
   std::vector<int> hostChunks;         // chunk sizes set by the caller (empty: planned)
   mutable std::vector<int> plannedChunks;   // the last plan, for plannedFor slices on plannedDev
   mutable int plannedFor = 0, plannedDev = -1;
   ~ctgpu_recon() {
     if (h_angles_pinned) cudaFreeHost(h_angles_pinned);
-    if (h_run_angles) {
-      if (runAngPending) cudaEventSynchronize(runAngEv);
-      cudaFreeHost(h_run_angles);
-    }
-    if (runAngEv) cudaEventDestroy(runAngEv);
     for (void* p : {(void*)d_spec, (void*)d_weights, (void*)d_filtered, (void*)d_angles,
                     (void*)d_views, (void*)d_scratch, (void*)d_sino, (void*)d_image,
                     (void*)d_bsino, (void*)d_bimage, (void*)d_filtered2, (void*)d_scratch2})
@@ -1441,22 +1429,8 @@ int ctgpu_recon_run(ctgpu_recon* r, const float* d_sino, int sinoPitch, const do
   RowsTarget rt;
   if (nViews > 0 && r->bproj != kDiff && r->bproj != kIDiff) {
     CUDA_TRY(ensure_device(r->d_angles, r->d_angles_cap, (size_t)nViews));
-    if (!r->runAngEv) CUDA_TRY(cudaEventCreateWithFlags(&r->runAngEv, cudaEventDisableTiming));
-    if (r->runAngPending) CUDA_TRY(cudaEventSynchronize(r->runAngEv));   // the last upload is done
-    r->runAngPending = false;
-    if (r->h_run_angles_cap < (size_t)nViews) {
-      if (r->h_run_angles) cudaFreeHost(r->h_run_angles);
-      r->h_run_angles = nullptr;
-      r->h_run_angles_cap = 0;
-      CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&r->h_run_angles), sizeof(double) * nViews,
-                             cudaHostAllocDefault));
-      r->h_run_angles_cap = nViews;
-    }
-    std::memcpy(r->h_run_angles, h_angles + startView, sizeof(double) * nViews);
-    CUDA_TRY(cudaMemcpyAsync(r->d_angles, r->h_run_angles, sizeof(double) * nViews,
+    CUDA_TRY(cudaMemcpyAsync(r->d_angles, h_angles + startView, sizeof(double) * nViews,
                              cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaEventRecord(r->runAngEv, st));
-    r->runAngPending = true;
     BackprojLaunch L = make_launch(r, nViews, r->pitch, r->d_angles, r->d_filtered, d_image,
                                    acc ? 1 : 0, scale, 1, 0, 0);
     CUDA_TRY(set_view_groups(r, L));
