@@ -300,16 +300,24 @@ static void pelem_setup(ora_pelem* e) {
 
 int ora_phantom_init(ora_phantom* p, int maxElems) {
   memset(p, 0, sizeof(*p));
-  p->e = calloc(maxElems > 0 ? maxElems : 1, sizeof(ora_pelem));
+  p->cap = maxElems > 0 ? maxElems : 1;
+  p->e = calloc((size_t)p->cap, sizeof(ora_pelem));
   p->xmin = 1E30; p->xmax = -1E30; p->ymin = 1E30; p->ymax = -1E30;   /* phantom.cpp:71-81 */
   return p->e != NULL;
 }
-void ora_phantom_free(ora_phantom* p) { free(p->e); p->e = NULL; p->n = 0; }
+void ora_phantom_free(ora_phantom* p) { free(p->e); p->e = NULL; p->n = 0; p->cap = 0; }
 
 /* Phantom::addPElem: list push_front, limits union (phantom.cpp:237-256) */
 int ora_phantom_add(ora_phantom* p, int type, double cx, double cy, double u, double v,
                     double rotDeg, double atten) {
   if (type == ORA_PELEM_INVALID) return 0;
+  if (p->n >= p->cap) {   /* room for one more: double the array */
+    const int cap = 2 * (p->cap > 0 ? p->cap : 1);
+    ora_pelem* e = realloc(p->e, (size_t)cap * sizeof(ora_pelem));
+    if (!e) return 0;
+    p->e = e;
+    p->cap = cap;
+  }
   memmove(&p->e[1], &p->e[0], (size_t)p->n * sizeof(ora_pelem));
   ora_pelem* e = &p->e[0];
   memset(e, 0, sizeof(*e));

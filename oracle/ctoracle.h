@@ -40,6 +40,7 @@ typedef struct {
 typedef struct {
   int n;               /* number of elements */
   int unit_pulse;      /* composition P_UNIT_PULSE */
+  int cap;             /* elements e has room for (grown by ora_phantom_add) */
   ora_pelem* e;        /* in the reference's list order (last added first) */
   double xmin, xmax, ymin, ymax;
 } ora_phantom;

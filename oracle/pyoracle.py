@@ -26,7 +26,8 @@ class _PElem(C.Structure):
 
 
 class _Phantom(C.Structure):
-    _fields_ = [("n", C.c_int), ("unit_pulse", C.c_int), ("e", C.POINTER(_PElem)),
+    _fields_ = [("n", C.c_int), ("unit_pulse", C.c_int), ("cap", C.c_int),
+                ("e", C.POINTER(_PElem)),
                 ("xmin", C.c_double), ("xmax", C.c_double), ("ymin", C.c_double),
                 ("ymax", C.c_double)]
 

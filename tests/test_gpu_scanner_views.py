@@ -81,3 +81,24 @@ def test_ellipsoid_scans_share_the_views(gpu):
     sc = scanner()
     for z0, dz in ((-1.0, 2.0 / nv), (-0.5, 1.0 / nv), (-1.0, 2.0 / nv)):
         assert torch.equal(scan(sc, z0, dz), scan(scanner(), z0, dz)), (z0, dz)
+
+
+@pytest.mark.parametrize("geo,ns,n_el", [("equiangular", 1, 150), ("parallel", 3, 60),
+                                         ("equilinear", 1, 500)])
+def test_large_phantoms_against_oracle(gpu, oracle, geo, ns, n_el):
+    """Phantoms with enough elements that a ray block holds fewer views (or
+    opts in to more than 48 KB of shared memory for one view), against the
+    FP64 oracle, with a view count no multiple of the views per block."""
+    torch, cg, device, phantoms = gpu
+    nd, nv = 97, 75
+    elems = phantoms.random_ellipses(seed=n_el, n=n_el)
+    sc = cg.Scanner(phantoms.make_phantom(elems), geo, nd, nv, nSample=ns)
+    sino = device.alloc_sinogram(nv, nd)
+    ang = device.raysums(sc, phantoms.make_phantom(elems), sino)
+    cg.sync()
+    osc = oracle.Scanner(oracle.Phantom(elements=elems), geo, nd, nv, nsample=ns)
+    ref, a_ref = osc.collect()
+    s = sino[:, :nd].cpu().numpy().astype(np.float64)
+    err = float(np.linalg.norm(s - ref) / np.linalg.norm(ref))
+    assert np.array_equal(ang, a_ref)
+    assert err < 1e-5, err

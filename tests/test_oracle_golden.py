@@ -234,3 +234,21 @@ def test_oracle_roi_reconstructions_match_reference(oracle, golden):
                                    err_msg=str(d["%d/cfg" % k]))
         k += 1
     assert k == 6
+
+
+def test_oracle_phantom_grows_past_its_initial_room(oracle):
+    """A phantom of more elements than its initial room (256): the element list
+    grows, keeps the reference's order (last added first), and a ray's sum is
+    the sum of the elements' own sums."""
+    rng = np.random.default_rng(3)
+    elems = [("ellipse", float(x), float(y), 0.02, 0.03, 0.0, 1.0)
+             for x, y in rng.uniform(-0.9, 0.9, size=(600, 2))]
+    big = oracle.Phantom(elements=elems)
+    assert len(big.bboxes()) == 600
+    # the list's first element is the last one added
+    x0, y0 = elems[-1][1], elems[-1][2]
+    b = big.bboxes()[0]
+    assert b[0] <= x0 <= b[2] and b[1] <= y0 <= b[3]
+    total = big.raysum(-2.0, 0.1, 2.0, 0.1)
+    parts = sum(oracle.Phantom(elements=[e]).raysum(-2.0, 0.1, 2.0, 0.1) for e in elems)
+    assert abs(total - parts) <= 1e-12 * max(1.0, abs(parts))
