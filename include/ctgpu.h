@@ -108,7 +108,10 @@ typedef struct {
 typedef struct ctgpu_scanner ctgpu_scanner;
 
 /* Scanner::Scanner: rot_angle in radians (phm2pj passes fraction * 2*pi),
- * ratios as in tools/phm2pj.cpp (defaults 2, 2, 1, 1). */
+ * ratios as in tools/phm2pj.cpp (defaults 2, 2, 1, 1).  A scanner does not
+ * change after create; it keeps the ray geometry of the last view range it
+ * scanned in device memory (about 200 B per view) and rebuilds it only for
+ * another range. */
 int ctgpu_scanner_create(const ctgpu_phantom* p, const char* geometry_name, int n_det, int n_view,
                          int offset_view, int n_sample, double rot_angle,
                          double focal_length_ratio, double center_detector_ratio,
