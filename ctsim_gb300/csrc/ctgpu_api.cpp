@@ -2272,7 +2272,8 @@ static bool batch_table(const ctgpu_batch* b, const BatchShape& shape,
   return true;
 }
 
-// the problems' set-up launches as branches forked from and joined to s
+// the problems' filter launches (their records were built at create) as
+// branches forked from and joined to s
 static int batch_enqueue_prep(ctgpu_batch* b, cudaStream_t s) {
   CUDA_TRY(cudaEventRecord(b->fork, s));
   for (int k = 0; k < kSideStreams; k++) CUDA_TRY(cudaStreamWaitEvent(b->side[k], b->fork, 0));
