@@ -2265,6 +2265,7 @@ static bool batch_table(const ctgpu_batch* b, const BatchShape& shape,
     P.rpitch = e.prep.rpitch;
     P.elemBytes = e.prep.elemBytes;
     P.eps = e.prep.eps;
+    P.fan = e.prep.fan;
     P.tilesX = (e.L.nx + 31) / 32;
     P.cv = batch_views_per_stage(e.prep, shape);
     if (P.cv < 1) return false;

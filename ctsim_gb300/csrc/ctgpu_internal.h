@@ -263,12 +263,20 @@ constexpr int kBackprojTile = 32;   // image pixels per tile side
 
 // The table-family backprojection as set-up launches plus a main launch, for
 // the batched path (many problems of different sizes, one persistent launch).
+// Equiangular fan beams: the arctangent series' coefficients of z^3, z^5 and
+// z^7 times the detector scale c5 = 1/detInc (the records' c[5]), so that a
+// pixel's position is one Horner chain in z^2:
+//   q = f + z*(c5 + z^2*(a3 + z^2*(a5 + z^2*a7)))
+struct FanSeries {
+  float a3, a5, a7;
+};
 struct TablePrep {
   int kind;        // main-kernel variant: geometry, interpolation, arctangent
   int win;         // row elements staged per (tile, view)
   int rpitch;      // row elements per view
   int elemBytes;   // bytes per row element (4, 8 or 16)
   float eps;       // FP32 position margin around jumps of the result
+  FanSeries fan;   // equiangular: the scaled series coefficients
   size_t recBytes, rowBytes;   // scratch: the records, then the rows
 };
 bool table_prep_info(const BackprojLaunch& L, TablePrep* out);
@@ -287,6 +295,7 @@ struct BatchProblem {
   const void* rows;
   int kind, win, rpitch, elemBytes, cv, tilesX;
   float eps;
+  FanSeries fan;
 };
 struct BatchItem { int problem, tile; };
 struct BatchShape { int blocksPerSM, cvCap; };
