@@ -99,3 +99,32 @@ def test_fan_positions_in_one_batch(gpu, oracle, interp):
         assert np.isfinite(got).all(), case
         err = rel_l2(got, ref)
         assert err < 1e-5, (case, err)
+
+
+@pytest.mark.parametrize("geo", ["parallel", "equiangular", "equilinear"])
+@pytest.mark.parametrize("nd", [2, 3, 4])
+def test_few_detectors(gpu, oracle, geo, nd):
+    """Two to four detectors: the cubic rows are all linear end intervals
+    (libctsupport/interpolator.cpp:37-75), windows span the whole padded
+    row; every interpolation against the FP64 reconstruction."""
+    torch, cg, device, phantoms = gpu
+    elems = phantoms.random_ellipses(seed=3, n=5)
+    nv, n = 30, 20
+    sc = cg.Scanner(phantoms.make_phantom(elems), geo, nd, nv)
+    sino = device.alloc_sinogram(nv, nd)
+    ang = device.raysums(sc, phantoms.make_phantom(elems), sino)
+    cg.sync()
+    osc = oracle.Scanner(oracle.Phantom(elements=elems), geo, nd, nv, nsample=1)
+    for interp in ("nearest", "linear", "cubic"):
+        plan = device.ReconPlan(sc.geometry(), n, n, "abs_hamming", 0.54, "fft", 2, "direct",
+                                interp, 1, "table")
+        img = torch.full((n, n), float("nan"), device="cuda")
+        plan.run(sino, ang, img)
+        cg.sync()
+        ref = oracle.reconstruct(osc.geom(), sino[:, :nd].cpu().numpy(), ang, n, n,
+                                 filter_name="abs_hamming", param=0.54, method="fft", zeropad=2,
+                                 backproj="table", interp=interp)
+        got = img.cpu().numpy()
+        assert np.isfinite(got).all(), interp
+        tol = 1e-5 * float(np.abs(ref).max()) + 1e-7
+        assert float(np.abs(got - ref).max()) <= tol, interp
