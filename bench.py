@@ -942,7 +942,7 @@ def run_gpu(args):
             "algorithmic_bytes_per_launch": B * N_VIEW * N_DET * 8,
             "achieved_gbs": B * N_VIEW * N_DET * 8 / (filt_avg_ms / 1e3) / 1e9,
             "frac_hbm": B * N_VIEW * N_DET * 8 / (filt_avg_ms / 1e3) / 1e9 / hbm,
-            # the survey's FFT-filter constant per view: 2 x 2.5 N log2 N + 6 N
+            # FFT-filter FLOP per view: two transforms of 2.5 N log2 N and a 6 N product
             "flop_per_launch": B * N_VIEW * (2 * 2.5 * 2048 * 11 + 6 * 2048),
             "note": "two views per complex transform of length 2048; the launch of "
                     "ctgpu_recon_run_batch also writes the 16-byte interval rows"},

@@ -1,10 +1,10 @@
 // k_peaks.cu -- measured roofline denominators for the benchmark (libctpeaks.so).
 //
 // The backprojection's per-pixel-view work is FP32 arithmetic on rows staged in
-// shared memory, and the survey of this path asks for its rate as a fraction
-// of the FP32 FMA peak and of the gather bandwidth (shared memory and L2).  No
-// measured figure exists for those, so this library measures them on
-// the GPU it runs on, with CUDA events, best of several launches:
+// shared memory; its rate is reported as a fraction of the FP32 FMA peak and
+// of the gather bandwidth (shared memory and L2).  No measured figure
+// exists for those, so this library measures them on the GPU it runs on, with
+// CUDA events, best of several launches:
 //
 //   out[0]  scalar FFMA throughput, TFLOP/s (FMA = 2 FLOP), 8 independent
 //           chains per thread, 4 CTAs x 256 threads per SM

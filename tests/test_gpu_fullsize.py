@@ -53,7 +53,7 @@ def test_fan_beam_c2_full_size(gpu, oracle):
         a_ref, img)
     cg.sync()
     e_i = rel_l2(img.cpu().numpy(), i_ref)
-    print("C2: sinogram rel-L2 %.3g, image rel-L2 %.3g" % (e_s, e_i))
+    print("equiangular 733 x 720 -> 512^2: sinogram rel-L2 %.3g, image rel-L2 %.3g" % (e_s, e_i))
     assert e_i < 1e-5, e_i
 
 

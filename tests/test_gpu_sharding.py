@@ -4,8 +4,8 @@ and the partial images are summed in host memory by the all-reduce (the
 reference's MPI pjrec scheme, tools/pjrec.cpp:375-418).  No kernel of one rank
 waits on the other: the ranks meet only in the host-side sum.
 
-- One slice (sharding.reconstruct_sharded): the C1 workload (Shepp-Logan,
-  parallel 367 x 320, abs_bandlimit by convolution, table / linear, 256 x 256)
+- One slice (sharding.reconstruct_sharded): the Shepp-Logan slice
+  (parallel 367 x 320, abs_bandlimit by convolution, table / linear, 256 x 256)
   against the single-process plan.run to 1e-6 rel-L2 (FP32 summation order)
   and against the reference's FP64 image to 1e-5.
 - A batch of three equiangular slices sharded by view block
@@ -88,7 +88,7 @@ def test_two_ranks_on_one_gpu_match_single_process(golden, tmp_path):
     rec = golden("recons")
     e2 = rel_l2(out["sharded"], rec["0/image64"])
     e3 = rel_l2(out["batch_sharded"], out["batch_whole"])
-    print("sharded C1 vs single process %.3g, vs reference FP64 %.3g; batch %.3g" % (e1, e2, e3))
+    print("sharded Shepp-Logan slice vs single process %.3g, vs reference FP64 %.3g; batch %.3g" % (e1, e2, e3))
     assert e1 < 1e-6, e1
     assert e2 < 1e-5, e2
     assert e3 < 1e-6, e3
