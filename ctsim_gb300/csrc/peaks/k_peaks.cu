@@ -2,9 +2,9 @@
 //
 // The backprojection's per-pixel-view work is FP32 arithmetic on rows staged in
 // shared memory; its rate is reported as a fraction of the FP32 FMA peak and
-// of the gather bandwidth (shared memory and L2).  No measured figure
-// exists for those, so this library measures them on the GPU it runs on, with
-// CUDA events, best of several launches:
+// of the gather bandwidth (shared memory and L2).  This library measures
+// those peaks on the GPU it runs on, with CUDA events, best of several
+// launches:
 //
 //   out[0]  scalar FFMA throughput, TFLOP/s (FMA = 2 FLOP), 8 independent
 //           chains per thread, 4 CTAs x 256 threads per SM
