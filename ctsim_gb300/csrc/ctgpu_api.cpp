@@ -1095,14 +1095,14 @@ int ctgpu_collect_projections_host(ctgpu_scanner* s, const ctgpu_phantom* p, int
                                    double* h_angles) {
   if (!s || !p || !h_sino) return fail(CTGPU_ERR_INVALID, "null argument");
   if (storageOffset + nViews > s->nView) return fail(CTGPU_ERR_INVALID, "view range past nView");
-  int pitch = pitch_for(s->nDet);
+  // rows written densely (pitch nDet), so that they come down in one copy
+  const int pitch = s->nDet;
   CUDA_TRY(ensure_device(s->d_sino, s->d_sino_cap, (size_t)nViews * pitch));
   int rc = ctgpu_collect_projections(s, p, startView, nViews, offsetView, 0, s->d_sino, pitch,
                                      h_angles ? h_angles + storageOffset : nullptr, nullptr);
   if (rc) return rc;
-  CUDA_TRY(cudaMemcpy2D(h_sino + (size_t)storageOffset * s->nDet, sizeof(float) * s->nDet,
-                        s->d_sino, sizeof(float) * pitch, sizeof(float) * s->nDet, nViews,
-                        cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(h_sino + (size_t)storageOffset * s->nDet, s->d_sino,
+                      sizeof(float) * (size_t)nViews * s->nDet, cudaMemcpyDeviceToHost));
   return ctgpu_sync(nullptr);
 }
 
